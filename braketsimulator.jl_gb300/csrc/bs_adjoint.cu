@@ -1,0 +1,550 @@
+// Adjoint-method gradients of <H> for parameterised circuits.
+//
+// No reference counterpart: BraketSimulator.jl declares AdjointGradient
+// (src/results.jl:90-159) but rejects it at parse time (src/pragmas.jl:67-68).
+// Algorithm (Jones & Gacon, arXiv:2009.02823): forward |psi_L>, |lambda> = H|psi_L>,
+// then for l = L..1: gradient of gate l from <lambda| dU_l |psi_{l-1}>, and
+// psi <- U_l^dag psi, lambda <- U_l^dag lambda.  Gates exp(-i theta G/2) with a
+// Pauli-string generator G give dE/dtheta = Im <lambda|G|psi_l>; PhaseShift gives
+// -2 Im <lambda|P1|psi_l>.
+//
+// Both backward states are swept together: one tile sweep loads the same tile of
+// psi and lambda, applies the daggered gates of a run to both, and accumulates
+// the inner products of the run's parameterised gates before applying them.
+#include <algorithm>
+#include <complex>
+#include <cstring>
+#include <vector>
+#include "bs_internal.h"
+#include "bs_ff.cuh"
+
+namespace {
+
+constexpr int kAThreads = 256;
+
+struct PauliTerm {
+    uint64_t xm, zm;     // endian masks
+    int ph;              // nY mod 4
+    float ch, cl;        // coefficient as float-float
+};
+
+__device__ __forceinline__ cff f4c(float4 v) { return {v.x, v.y, v.z, v.w}; }
+__device__ __forceinline__ float4 c4f(const cff& c) { return make_float4(c.rh, c.rl, c.ih, c.il); }
+
+// lambda_i = sum_t c_t (-i)^ph_t (-1)^popc(i & zm_t) psi_{i ^ xm_t}
+__global__ void __launch_bounds__(kAThreads) k_pauli_sum(const double2* __restrict__ psi, double2* __restrict__ lam,
+                                                         int64_t n, const PauliTerm* __restrict__ terms, int nt) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        ffacc ar{0.f, 0.f}, ai{0.f, 0.f};
+        for (int t = 0; t < nt; t++) {
+            PauliTerm p = terms[t];
+            cff x = load_c128(psi[i ^ (int64_t)p.xm]);
+            int ph = p.ph + ((__popcll((unsigned long long)i & p.zm) & 1) ? 2 : 0);
+            // (-i)^ph: multiply x by i^(4-ph)
+            x = cmul_ipow(x, (4 - (ph & 3)) & 3);
+            acc_add(ar, p.ch, p.cl, x.rh, x.rl);
+            acc_add(ai, p.ch, p.cl, x.ih, x.il);
+        }
+        lam[i] = store_c128(cdone(ar, ai));
+    }
+}
+
+__device__ void block_sum2(double a, double b, double* out2) {
+    __shared__ double ra[kAThreads / 32], rb[kAThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) { ra[w] = a; rb[w] = b; }
+    __syncthreads();
+    if (w == 0) {
+        a = (l < (int)(blockDim.x >> 5)) ? ra[l] : 0.0;
+        b = (l < (int)(blockDim.x >> 5)) ? rb[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            b += __shfl_down_sync(0xffffffffu, b, o);
+        }
+        if (l == 0) { atomicAdd(out2, a); atomicAdd(out2 + 1, b); }
+    }
+}
+
+// <a|b> (complex) into out2[0..1]
+__global__ void __launch_bounds__(kAThreads) k_inner(const double2* __restrict__ a, const double2* __restrict__ b,
+                                                     int64_t n, double* __restrict__ out2) {
+    ffsum sr{0.f, 0.f}, si{0.f, 0.f};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        cff x = load_c128(a[i]), y = load_c128(b[i]);
+        ffacc r, m;
+        acc_first(r, x.rh, x.rl, y.rh, y.rl);
+        acc_add(r, x.ih, x.il, y.ih, y.il);
+        acc_first(m, x.rh, x.rl, y.ih, y.il);
+        acc_add(m, -x.ih, -x.il, y.rh, y.rl);
+        ff rr = acc_done(r), mm = acc_done(m);
+        fsum_add(sr, rr.h, rr.l);
+        fsum_add(si, mm.h, mm.l);
+    }
+    block_sum2(ff2d(sr.h, sr.l), ff2d(si.h, si.l), out2);
+}
+
+// Dual-state tile sweep for the backward pass.
+//   kind 0 dense / 1 diagonal / 2 monomial: applied to both psi and lambda tiles;
+//   kind 3 gradient marker: acc[slot] += w * Im <lambda|G|psi> over the tile, G a
+//          Pauli string (xm on tile-local bits, zm on global bits, phase ph) or,
+//          when k == 1, the projector P1 on global bit gbit[0].
+struct AdjGate {
+    TileGate g;
+    uint32_t xm_local;
+    int32_t ph;
+    uint64_t zm;
+    int32_t slot;
+    int32_t projector;
+    double weight;
+};
+
+template <int K>
+__device__ void adj_dense(float4* sm, int T, const TileGate& g, const float4* __restrict__ mats) {
+    constexpr int D = 1 << K;
+    int pos[K];
+    for (int q = 0; q < K; q++) pos[q] = g.tbit[q];
+    for (int a = 0; a < K; a++)
+        for (int b = a + 1; b < K; b++)
+            if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
+    const int ngroups = 1 << (T - K);
+    const float4* m = mats + g.mat_off;
+    for (int gr = threadIdx.x; gr < ngroups; gr += blockDim.x) {
+        int jb = gr;
+        for (int q = 0; q < K; q++) { int low = jb & ((1 << pos[q]) - 1); jb = ((jb >> pos[q]) << (pos[q] + 1)) | low; }
+        if ((jb & (int)g.lc_mask) != (int)g.lc_val) continue;
+        cff x[D];
+        int idx[D];
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+            int j = jb;
+            for (int q = 0; q < K; q++) if ((c >> q) & 1) j |= 1 << g.tbit[q];
+            idx[c] = j;
+            x[c] = f4c(sm[j]);
+        }
+#pragma unroll
+        for (int r = 0; r < D; r++) {
+            ffacc ar, ai;
+            cmac_first(ar, ai, f4c(__ldg(m + r * D)), x[0]);
+#pragma unroll
+            for (int c = 1; c < D; c++) cmac(ar, ai, f4c(__ldg(m + r * D + c)), x[c]);
+            sm[idx[r]] = c4f(cdone(ar, ai));
+        }
+    }
+}
+
+__device__ void adj_apply(float4* sm, int T, int L, const TileGate& g, const float4* mats, const int32_t* perms,
+                          int64_t base, const int64_t* off_tab) {
+    const int nt = 1 << T, lowmask = (1 << L) - 1;
+    if (g.kind == 1) {
+        const float4* m = mats + g.mat_off;
+        for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+            if ((j & (int)g.lc_mask) != (int)g.lc_val) continue;
+            int64_t gi = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+            int di = 0;
+            for (int q = 0; q < g.k; q++) di |= (int)((gi >> g.gbit[q]) & 1) << q;
+            sm[j] = c4f(cmul(f4c(__ldg(m + di)), f4c(sm[j])));
+        }
+    } else if (g.kind == 0) {
+        switch (g.k) {
+            case 1: adj_dense<1>(sm, T, g, mats); break;
+            case 2: adj_dense<2>(sm, T, g, mats); break;
+            case 3: adj_dense<3>(sm, T, g, mats); break;
+            default: adj_dense<4>(sm, T, g, mats); break;
+        }
+    } else {
+        // monomial
+        const int D = 1 << g.k;
+        int pos[BS_TILE_MAXK];
+        for (int q = 0; q < g.k; q++) pos[q] = g.tbit[q];
+        for (int a = 0; a < g.k; a++)
+            for (int b = a + 1; b < g.k; b++)
+                if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
+        const int32_t* p = perms + g.perm_off;
+        for (int gr = threadIdx.x; gr < (1 << (T - g.k)); gr += blockDim.x) {
+            int jb = gr;
+            for (int q = 0; q < g.k; q++) { int low = jb & ((1 << pos[q]) - 1); jb = ((jb >> pos[q]) << (pos[q] + 1)) | low; }
+            if ((jb & (int)g.lc_mask) != (int)g.lc_val) continue;
+            float4 x[16];
+            int idx[16];
+            for (int c = 0; c < D; c++) {
+                int j = jb;
+                for (int q = 0; q < g.k; q++) if ((c >> q) & 1) j |= 1 << g.tbit[q];
+                idx[c] = j;
+                x[c] = sm[j];
+            }
+            for (int c = 0; c < D; c++) sm[idx[__ldg(p + 2 * c)]] = c4f(cmul_ipow(f4c(x[c]), __ldg(p + 2 * c + 1)));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kAThreads) k_adjoint_sweep(double2* __restrict__ psi, double2* __restrict__ lam,
+                                                             SweepDesc d, const AdjGate* __restrict__ ag,
+                                                             double* __restrict__ grad_acc, int64_t tile0) {
+    extern __shared__ float4 smem[];
+    const int T = d.T, L = d.L, H = T - L;
+    const int nt = 1 << T;
+    float4* sp = smem;
+    float4* sl = smem + nt;
+    int64_t* off_tab = reinterpret_cast<int64_t*>(smem + 2 * nt);
+    __shared__ int64_t s_base;
+    const int64_t tile = tile0 + (int64_t)blockIdx.x;
+    if (threadIdx.x == 0) {
+        int64_t base = 0;
+        int src = 0;
+        for (int bit = 0; bit < d.n_bits; bit++)
+            if (!((d.tile_mask >> bit) & 1ULL)) { base |= ((tile >> src) & 1LL) << bit; src++; }
+        s_base = base;
+    }
+    for (int i = threadIdx.x; i < (1 << H); i += blockDim.x) {
+        int64_t o = 0;
+        for (int j = 0; j < H; j++) if ((i >> j) & 1) o |= 1LL << d.hi_bits[j];
+        off_tab[i] = o;
+    }
+    __syncthreads();
+    const int64_t base = s_base;
+    const int lowmask = (1 << L) - 1;
+    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+        sp[j] = c4f(load_c128(psi[gidx]));
+        sl[j] = c4f(load_c128(lam[gidx]));
+    }
+    __syncthreads();
+    for (int gi = 0; gi < d.n_gates; gi++) {
+        const AdjGate a = ag[gi];
+        if (a.g.kind == 3) {
+            // Im <lambda| G |psi> over the tile
+            ffsum acc{0.f, 0.f};
+            for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+                int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+                cff l = f4c(sl[j]);
+                cff x;
+                if (a.projector) {
+                    if (!((gidx >> a.g.gbit[0]) & 1)) continue;
+                    x = f4c(sp[j]);
+                } else {
+                    x = f4c(sp[j ^ (int)a.xm_local]);
+                    int ph = a.ph + ((__popcll((unsigned long long)gidx & a.zm) & 1) ? 2 : 0);
+                    x = cmul_ipow(x, (4 - (ph & 3)) & 3);
+                }
+                // Im(conj(l) * x) = l.r x.i - l.i x.r
+                ffacc m;
+                acc_first(m, l.rh, l.rl, x.ih, x.il);
+                acc_add(m, -l.ih, -l.il, x.rh, x.rl);
+                ff v = acc_done(m);
+                fsum_add(acc, v.h, v.l);
+            }
+            double v = ff2d(acc.h, acc.l) * a.weight;
+            __shared__ double red[kAThreads / 32];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double s = 0.0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
+                atomicAdd(grad_acc + a.slot, s);
+            }
+            __syncthreads();
+            continue;
+        }
+        if ((base & (int64_t)a.g.gc_mask) != (int64_t)a.g.gc_val) continue;
+        adj_apply(sp, T, L, a.g, d.mats, d.perms, base, off_tab);
+        adj_apply(sl, T, L, a.g, d.mats, d.perms, base, off_tab);
+        __syncthreads();
+    }
+    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+        psi[gidx] = store_c128(f4c(sp[j]));
+        lam[gidx] = store_c128(f4c(sl[j]));
+    }
+}
+
+inline float4 to_cff(double re, double im) {
+    float4 v;
+    v.x = (float)re; v.y = (float)(re - (double)v.x);
+    v.z = (float)im; v.w = (float)(im - (double)v.z);
+    return v;
+}
+
+struct BwdItem {          // one element of the reversed gate list
+    HostGate g;
+    bool marker = false;
+    int slot = 0;
+    int projector = 0;
+    uint64_t xm = 0, zm = 0;   // endian masks of the generator
+    int ph = 0;
+    double weight = 1.0;
+};
+
+// U^dagger of a lowered gate (same targets and controls)
+HostGate dagger(const HostGate& h) {
+    HostGate d = h;
+    const int D = 1 << h.k;
+    if (h.kind == 1) {
+        for (int i = 0; i < D; i++) d.mat[2 * i + 1] = -h.mat[2 * i + 1];
+    } else if (h.kind == 0) {
+        for (int r = 0; r < D; r++)
+            for (int c = 0; c < D; c++) {
+                d.mat[2 * (r * D + c)] = h.mat[2 * (c * D + r)];
+                d.mat[2 * (r * D + c) + 1] = -h.mat[2 * (c * D + r) + 1];
+            }
+    } else {
+        // column c -> row r with phase p  ==>  column r -> row c with phase -p
+        for (int c = 0; c < D; c++) {
+            int r = h.perm[2 * c], p = h.perm[2 * c + 1];
+            d.perm[2 * r] = c;
+            d.perm[2 * r + 1] = (4 - p) & 3;
+        }
+    }
+    return d;
+}
+
+}  // namespace
+
+extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, const int32_t* param_index,
+                                   const int32_t* gen_kind, const uint64_t* gen_xmask, const uint64_t* gen_zmask,
+                                   int n_params, int n_terms, const uint64_t* xmask, const uint64_t* zmask,
+                                   const double* coeffs, double* energy_out, double* grad_out) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (s->kind != BS_KIND_SV) return bs_fail(s, BS_ERR_UNSUPPORTED, "adjoint gradients need a state-vector simulator");
+    if (n_ops < 0 || (n_ops && (!ops || !param_index || !gen_kind || !gen_xmask || !gen_zmask)) || n_params < 0 ||
+        n_terms < 1 || !xmask || !zmask || !coeffs || !energy_out || (n_params && !grad_out))
+        return bs_fail(s, BS_ERR_INVALID_ARG, "bad adjoint arguments");
+    const int n = s->n;
+    const int64_t len = s->len;
+    auto to_endian = [n](uint64_t m) {
+        uint64_t e = 0;
+        for (int q = 0; q < n; q++) if ((m >> q) & 1ULL) e |= 1ULL << (n - 1 - q);
+        return e;
+    };
+    // 1. forward pass
+    int rc = bs_evolve(s, ops, n_ops, 0);
+    if (rc) return rc;
+    cudaEventRecord(s->ev0, s->stream);
+    // 2. lambda = H psi
+    void* lam = nullptr;
+    rc = bs_cuda_check(s, cudaMallocAsync(&lam, (size_t)len * 16, s->stream), "lambda allocation");
+    if (rc) return rc;
+    std::vector<PauliTerm> terms((size_t)n_terms);
+    for (int t = 0; t < n_terms; t++) {
+        uint64_t x = xmask[t], z = zmask[t];
+        int ny = __builtin_popcountll(x & z);
+        terms[(size_t)t].xm = to_endian(x);
+        terms[(size_t)t].zm = to_endian(z);
+        terms[(size_t)t].ph = ny & 3;
+        terms[(size_t)t].ch = (float)coeffs[t];
+        terms[(size_t)t].cl = (float)(coeffs[t] - (double)terms[(size_t)t].ch);
+    }
+    rc = bs_ensure_scratch(s, (int64_t)n_terms * (int64_t)sizeof(PauliTerm) + (int64_t)(n_params + 2) * 8 + 256);
+    if (rc) { cudaFreeAsync(lam, s->stream); return rc; }
+    PauliTerm* d_terms = (PauliTerm*)s->scratch;
+    double* d_acc = (double*)((char*)s->scratch + (((int64_t)n_terms * (int64_t)sizeof(PauliTerm) + 255) & ~255LL));
+    cudaMemcpyAsync(d_terms, terms.data(), terms.size() * sizeof(PauliTerm), cudaMemcpyHostToDevice, s->stream);
+    cudaMemsetAsync(d_acc, 0, (size_t)(n_params + 2) * 8, s->stream);
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((len + kAThreads - 1) / kAThreads, 152 * 8));
+    k_pauli_sum<<<blocks, kAThreads, 0, s->stream>>>((const double2*)s->state, (double2*)lam, len, d_terms, n_terms);
+    k_inner<<<blocks, kAThreads, 0, s->stream>>>((const double2*)s->state, (const double2*)lam, len, d_acc + n_params);
+    // 3. backward: reversed, daggered gate list with gradient markers before each parameterised gate
+    std::vector<BwdItem> items;
+    for (int64_t i = n_ops - 1; i >= 0; i--) {
+        const bs_op& op = ops[i];
+        if (op.kind != 0) continue;
+        std::vector<HostGate> hg;
+        rc = bs_lower_gate(s, op.matrix, op.n_targets, op.targets, op.n_controls, op.controls, op.control_values,
+                           op.flags, false, hg);
+        if (rc) { cudaFreeAsync(lam, s->stream); return rc; }
+        if (param_index[i] >= 0) {
+            if (param_index[i] >= n_params) { cudaFreeAsync(lam, s->stream); return bs_fail(s, BS_ERR_INVALID_ARG, "parameter index out of range"); }
+            BwdItem m;
+            m.marker = true;
+            m.slot = param_index[i];
+            m.projector = gen_kind[i] == 1;
+            if (m.projector) {
+                // PhaseShift on its target: weight -2, projector on the target's endian bit
+                m.g.k = 1;
+                m.g.ebit[0] = n - 1 - op.targets[0];
+                m.weight = -2.0;
+            } else {
+                m.xm = to_endian(gen_xmask[i]);
+                m.zm = to_endian(gen_zmask[i]);
+                m.ph = __builtin_popcountll(gen_xmask[i] & gen_zmask[i]) & 3;
+                m.g.k = 0;
+                for (int q = 0; q < n; q++)
+                    if ((m.xm >> q) & 1ULL) m.g.ebit[m.g.k++] = q;
+                m.weight = 1.0;
+            }
+            m.g.kind = 3;
+            items.push_back(m);
+        }
+        for (const HostGate& h : hg) {
+            BwdItem it;
+            it.g = dagger(h);
+            items.push_back(it);
+        }
+    }
+    // plan sweeps: markers need their flip bits in the tile, and they must not move
+    // past a gate sharing bits (they read the current psi and lambda)
+    const int n_bits = n;
+    const int T = std::min(BS_TILE_MAX_BITS, n_bits);
+    const int L = std::min(BS_TILE_LOW_BITS, T);
+    const int cap = T - L;
+    std::vector<std::vector<int>> sweeps_items;
+    std::vector<std::vector<int>> sweeps_hi;
+    {
+        const size_t G = items.size();
+        std::vector<char> done(G, 0);
+        size_t remaining = G, first = 0;
+        auto touch = [&](const BwdItem& it) {
+            uint64_t m = it.g.cmask | it.zm | it.xm;
+            for (int q = 0; q < it.g.k; q++) m |= 1ULL << it.g.ebit[q];
+            return m;
+        };
+        auto need = [&](const BwdItem& it) -> uint64_t {
+            uint64_t m = 0;
+            if (!it.marker && it.g.kind == 1) return m;
+            if (it.marker) return it.xm & ~(((uint64_t)1 << L) - 1);
+            for (int q = 0; q < it.g.k; q++) if (it.g.ebit[q] >= L) m |= 1ULL << it.g.ebit[q];
+            return m;
+        };
+        while (remaining) {
+            std::vector<int> idx;
+            uint64_t chosen = 0, blocked = 0;
+            int nch = 0;
+            for (size_t i = first; i < G; i++) {
+                if (done[i]) continue;
+                uint64_t t = touch(items[i]);
+                if (t & blocked) { blocked |= t; continue; }
+                uint64_t nb = need(items[i]) & ~chosen;
+                int add = __builtin_popcountll(nb);
+                bool too_big = !items[i].marker && items[i].g.kind != 1 &&
+                               (items[i].g.k > BS_TILE_MAXK || __builtin_popcountll(need(items[i])) > cap);
+                if (too_big || (items[i].marker && __builtin_popcountll(need(items[i])) > cap)) {
+                    cudaFreeAsync(lam, s->stream);
+                    return bs_fail(s, BS_ERR_UNSUPPORTED, "adjoint gate too wide for a tile");
+                }
+                if (nch + add <= cap) {
+                    chosen |= nb;
+                    nch += add;
+                    idx.push_back((int)i);
+                    done[i] = 1;
+                    remaining--;
+                } else {
+                    blocked |= t;
+                }
+            }
+            while (first < G && done[first]) first++;
+            std::vector<int> hi;
+            for (int b = L; b < n_bits; b++) if ((chosen >> b) & 1ULL) hi.push_back(b);
+            for (int b = L; b < n_bits && (int)hi.size() < cap; b++) if (!((chosen >> b) & 1ULL)) hi.push_back(b);
+            std::sort(hi.begin(), hi.end());
+            sweeps_items.push_back(idx);
+            sweeps_hi.push_back(hi);
+        }
+    }
+    // pack device data
+    std::vector<AdjGate> ag;
+    std::vector<float4> mats;
+    std::vector<int32_t> perms;
+    std::vector<int64_t> sweep_first;
+    for (size_t sw = 0; sw < sweeps_items.size(); sw++) {
+        int local[64];
+        for (int b = 0; b < 64; b++) local[b] = -1;
+        for (int b = 0; b < L; b++) local[b] = b;
+        for (size_t i = 0; i < sweeps_hi[sw].size(); i++) local[sweeps_hi[sw][i]] = L + (int)i;
+        sweep_first.push_back((int64_t)ag.size());
+        for (int ii : sweeps_items[sw]) {
+            const BwdItem& it = items[(size_t)ii];
+            AdjGate a{};
+            a.g.kind = it.marker ? 3 : it.g.kind;
+            a.g.k = it.g.k;
+            if (it.marker) {
+                a.slot = it.slot;
+                a.projector = it.projector;
+                a.weight = it.weight;
+                a.zm = it.zm;
+                a.ph = it.ph;
+                uint32_t xl = 0;
+                for (int b = 0; b < n_bits; b++) if ((it.xm >> b) & 1ULL) xl |= 1u << local[b];
+                a.xm_local = xl;
+                if (it.projector) a.g.gbit[0] = it.g.ebit[0];
+                ag.push_back(a);
+                continue;
+            }
+            const HostGate& hg = it.g;
+            uint64_t gcm = 0, gcv = 0;
+            uint32_t lcm = 0, lcv = 0;
+            for (int b = 0; b < n_bits; b++) {
+                if (!((hg.cmask >> b) & 1ULL)) continue;
+                uint64_t v = (hg.cval >> b) & 1ULL;
+                if (local[b] >= 0) { lcm |= 1u << local[b]; lcv |= (uint32_t)v << local[b]; }
+                else { gcm |= 1ULL << b; gcv |= v << b; }
+            }
+            a.g.lc_mask = lcm; a.g.lc_val = lcv; a.g.gc_mask = gcm; a.g.gc_val = gcv;
+            for (int q = 0; q < hg.k; q++) {
+                a.g.gbit[q] = hg.ebit[q];
+                if (q < BS_TILE_MAXK) a.g.tbit[q] = local[hg.ebit[q]];
+            }
+            a.g.mat_off = (int32_t)mats.size();
+            a.g.perm_off = (int32_t)perms.size();
+            if (hg.kind == 0) for (int e = 0; e < (1 << (2 * hg.k)); e++) mats.push_back(to_cff(hg.mat[2 * e], hg.mat[2 * e + 1]));
+            else if (hg.kind == 1) for (int e = 0; e < (1 << hg.k); e++) mats.push_back(to_cff(hg.mat[2 * e], hg.mat[2 * e + 1]));
+            else perms.insert(perms.end(), hg.perm.begin(), hg.perm.end());
+            ag.push_back(a);
+        }
+    }
+    sweep_first.push_back((int64_t)ag.size());
+    auto al = [](int64_t x) { return (x + 255) & ~(int64_t)255; };
+    const int64_t b_ag = al((int64_t)ag.size() * (int64_t)sizeof(AdjGate));
+    const int64_t b_m = al((int64_t)mats.size() * (int64_t)sizeof(float4));
+    const int64_t b_p = al((int64_t)(perms.size() + 1) * 4);
+    rc = bs_ensure_plan(s, b_ag + b_m + b_p);
+    if (rc) { cudaFreeAsync(lam, s->stream); return rc; }
+    std::vector<char> host((size_t)(b_ag + b_m + b_p), 0);
+    if (!ag.empty()) std::memcpy(host.data(), ag.data(), ag.size() * sizeof(AdjGate));
+    if (!mats.empty()) std::memcpy(host.data() + b_ag, mats.data(), mats.size() * sizeof(float4));
+    if (!perms.empty()) std::memcpy(host.data() + b_ag + b_m, perms.data(), perms.size() * 4);
+    cudaMemcpyAsync(s->plan_buf, host.data(), host.size(), cudaMemcpyHostToDevice, s->stream);
+    const AdjGate* d_ag = (const AdjGate*)s->plan_buf;
+    const float4* d_m = (const float4*)((char*)s->plan_buf + b_ag);
+    const int32_t* d_p = (const int32_t*)((char*)s->plan_buf + b_ag + b_m);
+    const int H = T - L;
+    const size_t smem = (size_t)2 * ((size_t)1 << T) * sizeof(float4) + ((size_t)1 << H) * sizeof(int64_t);
+    cudaFuncSetAttribute(k_adjoint_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    const int64_t ntiles = (int64_t)1 << (n_bits - T);
+    for (size_t sw = 0; sw < sweeps_items.size(); sw++) {
+        SweepDesc d{};
+        d.n_bits = n_bits;
+        d.T = T;
+        d.L = L;
+        d.n_gates = (int)(sweep_first[sw + 1] - sweep_first[sw]);
+        uint64_t tm = (1ULL << L) - 1;
+        for (int i = 0; i < H; i++) { d.hi_bits[i] = sweeps_hi[sw][(size_t)i]; tm |= 1ULL << sweeps_hi[sw][(size_t)i]; }
+        d.tile_mask = tm;
+        d.mats = d_m;
+        d.perms = d_p;
+        for (int64_t t0 = 0; t0 < ntiles; t0 += (1LL << 30)) {
+            int64_t nb = std::min<int64_t>(ntiles - t0, 1LL << 30);
+            k_adjoint_sweep<<<(unsigned)nb, kAThreads, smem, s->stream>>>((double2*)s->state, (double2*)lam, d,
+                                                                           d_ag + sweep_first[sw], d_acc, t0);
+        }
+        s->stats.kernel_launches++;
+        s->stats.sweeps++;
+        s->stats.bytes_moved += 64.0 * (double)len;
+    }
+    std::vector<double> res((size_t)n_params + 2);
+    cudaMemcpyAsync(res.data(), d_acc, res.size() * 8, cudaMemcpyDeviceToHost, s->stream);
+    cudaFreeAsync(lam, s->stream);
+    cudaEventRecord(s->ev1, s->stream);
+    rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "adjoint");
+    if (rc) return rc;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    s->stats.gpu_ms += ms;
+    *energy_out = res[(size_t)n_params];
+    for (int p = 0; p < n_params; p++) grad_out[p] = res[(size_t)p];
+    return BS_OK;
+}

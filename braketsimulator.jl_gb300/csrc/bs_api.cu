@@ -1,0 +1,266 @@
+// C ABI entry points: handle lifecycle, state transfer, gate / channel / evolve.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include "bs_internal.h"
+
+int bs_fail(bs_sim* s, int code, const std::string& msg) {
+    if (s) s->err = msg;
+    return code;
+}
+int bs_cuda_check(bs_sim* s, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return BS_OK;
+    return bs_fail(s, e == cudaErrorMemoryAllocation ? BS_ERR_ALLOC : BS_ERR_CUDA,
+                   std::string(what) + ": " + cudaGetErrorString(e));
+}
+int bs_vec_bits(const bs_sim* s) { return s->kind == BS_KIND_DM ? 2 * s->n : s->n; }
+
+int bs_ensure_scratch(bs_sim* s, int64_t bytes) {
+    if (s->scratch_bytes >= bytes) return BS_OK;
+    if (s->scratch) cudaFree(s->scratch);
+    s->scratch = nullptr;
+    s->scratch_bytes = 0;
+    int rc = bs_cuda_check(s, cudaMalloc(&s->scratch, (size_t)bytes), "scratch allocation");
+    if (rc) return rc;
+    s->scratch_bytes = bytes;
+    return BS_OK;
+}
+int bs_ensure_plan(bs_sim* s, int64_t bytes) {
+    if (s->plan_bytes >= bytes) return BS_OK;
+    // the previous plan may still be read by queued kernels
+    cudaStreamSynchronize(s->stream);
+    if (s->plan_buf) cudaFree(s->plan_buf);
+    s->plan_buf = nullptr;
+    s->plan_bytes = 0;
+    int64_t b = std::max<int64_t>(bytes, 1 << 16);
+    int rc = bs_cuda_check(s, cudaMalloc(&s->plan_buf, (size_t)b), "plan allocation");
+    if (rc) return rc;
+    s->plan_bytes = b;
+    return BS_OK;
+}
+
+namespace {
+
+__global__ void k_basis0(double2* psi) { psi[0] = make_double2(1.0, 0.0); }
+
+int alloc_state(bs_sim* s, int n) {
+    const int bits = (s->kind == BS_KIND_DM) ? 2 * n : n;
+    if (n < 0 || bits > 34) return bs_fail(s, BS_ERR_INVALID_ARG, "qubit count out of range");
+    const int64_t len = (int64_t)1 << bits;
+    const int64_t bytes = len * 16;
+    if (bytes > s->cap_bytes) {
+        if (s->state) cudaFree(s->state);
+        s->state = nullptr;
+        s->cap_bytes = 0;
+        int rc = bs_cuda_check(s, cudaMalloc(&s->state, (size_t)bytes), "state allocation");
+        if (rc) return rc;
+        s->cap_bytes = bytes;
+    }
+    s->n = n;
+    s->len = len;
+    s->alias_valid = false;
+    int rc = bs_cuda_check(s, cudaMemsetAsync(s->state, 0, (size_t)bytes, s->stream), "state clear");
+    if (rc) return rc;
+    k_basis0<<<1, 1, 0, s->stream>>>((double2*)s->state);
+    return bs_cuda_check(s, cudaGetLastError(), "state init");
+}
+
+bool ok_handle(bs_sim* s) { return s != nullptr; }
+
+}  // namespace
+
+extern "C" {
+
+const char* bs_version(void) { return "braket_gb300 0.1 (sm_103a, float-float complex128)"; }
+
+int bs_create(int kind, int n_qubits, int precision, bs_sim** out) {
+    if (!out) return BS_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (kind != BS_KIND_SV && kind != BS_KIND_DM) return BS_ERR_INVALID_ARG;
+    if (precision != BS_PREC_C128) return BS_ERR_UNSUPPORTED;
+    bs_sim* s = new (std::nothrow) bs_sim();
+    if (!s) return BS_ERR_ALLOC;
+    s->kind = kind;
+    s->precision = precision;
+    cudaGetDevice(&s->device);
+    int rc = bs_cuda_check(s, cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream");
+    if (!rc) rc = bs_cuda_check(s, cudaEventCreate(&s->ev0), "event");
+    if (!rc) rc = bs_cuda_check(s, cudaEventCreate(&s->ev1), "event");
+    if (!rc) rc = alloc_state(s, n_qubits);
+    if (rc) { bs_destroy(s); return rc; }
+    *out = s;
+    return BS_OK;
+}
+
+int bs_destroy(bs_sim* s) {
+    if (!s) return BS_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->state) cudaFree(s->state);
+    if (s->scratch) cudaFree(s->scratch);
+    if (s->plan_buf) cudaFree(s->plan_buf);
+    if (s->alias_ap) cudaFree(s->alias_ap);
+    if (s->alias_ix) cudaFree(s->alias_ix);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return BS_OK;
+}
+
+int bs_reinit(bs_sim* s, int n_qubits) {
+    if (!ok_handle(s)) return BS_ERR_INVALID_ARG;
+    return alloc_state(s, n_qubits);
+}
+
+int bs_qubit_count(const bs_sim* s, int* out) {
+    if (!s || !out) return BS_ERR_INVALID_ARG;
+    *out = s->n;
+    return BS_OK;
+}
+
+const char* bs_last_error(const bs_sim* s) { return s ? s->err.c_str() : "null handle"; }
+
+int bs_set_state(bs_sim* s, const double* host, int64_t n) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (!host || n != s->len) return bs_fail(s, BS_ERR_INVALID_ARG, "state length mismatch");
+    s->alias_valid = false;
+    int rc = bs_cuda_check(s, cudaMemcpyAsync(s->state, host, (size_t)n * 16, cudaMemcpyHostToDevice, s->stream), "set_state");
+    if (rc) return rc;
+    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "set_state sync");
+}
+
+int bs_get_state(bs_sim* s, double* host, int64_t n) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (!host || n != s->len) return bs_fail(s, BS_ERR_INVALID_ARG, "state length mismatch");
+    int rc = bs_cuda_check(s, cudaMemcpyAsync(host, s->state, (size_t)n * 16, cudaMemcpyDeviceToHost, s->stream), "get_state");
+    if (rc) return rc;
+    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "get_state sync");
+}
+
+int bs_set_state_device(bs_sim* s, const void* dev, int64_t n) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (!dev || n != s->len) return bs_fail(s, BS_ERR_INVALID_ARG, "state length mismatch");
+    s->alias_valid = false;
+    return bs_cuda_check(s, cudaMemcpyAsync(s->state, dev, (size_t)n * 16, cudaMemcpyDeviceToDevice, s->stream), "set_state_device");
+}
+
+int bs_get_state_device(bs_sim* s, void* dev, int64_t n) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (!dev || n != s->len) return bs_fail(s, BS_ERR_INVALID_ARG, "state length mismatch");
+    return bs_cuda_check(s, cudaMemcpyAsync(dev, s->state, (size_t)n * 16, cudaMemcpyDeviceToDevice, s->stream), "get_state_device");
+}
+
+int bs_copy_state(bs_sim* dst, const bs_sim* src) {
+    if (!dst || !src) return BS_ERR_INVALID_ARG;
+    if (dst->kind != src->kind || dst->len != src->len) return bs_fail(dst, BS_ERR_INVALID_ARG, "simulators differ in kind or size");
+    cudaStreamSynchronize(src->stream);
+    dst->alias_valid = false;
+    return bs_cuda_check(dst, cudaMemcpyAsync(dst->state, src->state, (size_t)dst->len * 16, cudaMemcpyDeviceToDevice, dst->stream), "copy_state");
+}
+
+int bs_synchronize(bs_sim* s) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "synchronize");
+}
+
+int bs_state_device_ptr(bs_sim* s, void** out) {
+    if (!s || !out) return BS_ERR_INVALID_ARG;
+    *out = s->state;
+    return BS_OK;
+}
+
+int bs_last_stats(const bs_sim* s, bs_stats* out) {
+    if (!s || !out) return BS_ERR_INVALID_ARG;
+    *out = s->stats;
+    return BS_OK;
+}
+
+int bs_apply_gate(bs_sim* s, const double* matrix, int k, const int* targets, int nc, const int* controls,
+                  const int* cvals, unsigned flags) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    std::vector<HostGate> hg;
+    int rc = bs_lower_gate(s, matrix, k, targets, nc, controls, cvals, flags, s->kind == BS_KIND_DM, hg);
+    if (rc) return rc;
+    std::vector<Sweep> sw;
+    bs_plan_sweeps(hg, bs_vec_bits(s), sw);
+    s->alias_valid = false;
+    return bs_run_sweeps(s, sw);
+}
+
+int bs_dm_apply_vec_gate(bs_sim* s, const double* matrix, int k, const int* targets, int nc, const int* controls,
+                         const int* cvals, unsigned flags) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (s->kind != BS_KIND_DM) return bs_fail(s, BS_ERR_STATE, "vec gate needs a density-matrix simulator");
+    std::vector<HostGate> hg;
+    int rc = bs_lower_gate(s, matrix, k, targets, nc, controls, cvals, flags, false, hg);
+    if (rc) return rc;
+    std::vector<Sweep> sw;
+    bs_plan_sweeps(hg, bs_vec_bits(s), sw);
+    s->alias_valid = false;
+    return bs_run_sweeps(s, sw);
+}
+
+int bs_apply_kraus(bs_sim* s, const double* kraus, int nk, int k, const int* targets, unsigned flags) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (s->kind != BS_KIND_DM) return bs_fail(s, BS_ERR_STATE, "noise needs a density-matrix simulator");
+    if (!kraus || !targets) return bs_fail(s, BS_ERR_INVALID_ARG, "null argument");
+    s->alias_valid = false;
+    if (flags & BS_NOISE_PHYSICAL) {
+        std::vector<HostGate> hg;
+        int rc = bs_lower_kraus_physical(s, kraus, nk, k, targets, flags, hg);
+        if (rc) return rc;
+        std::vector<Sweep> sw;
+        bs_plan_sweeps(hg, bs_vec_bits(s), sw);
+        return bs_run_sweeps(s, sw);
+    }
+    return bs_kraus_reference(s, kraus, nk, k, targets, flags);
+}
+
+int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (n_ops < 0 || (n_ops > 0 && !ops)) return bs_fail(s, BS_ERR_INVALID_ARG, "bad op list");
+    s->stats = bs_stats{};
+    s->alias_valid = false;
+    cudaEventRecord(s->ev0, s->stream);
+    std::vector<HostGate> pending;
+    auto flush = [&]() -> int {
+        if (pending.empty()) return BS_OK;
+        std::vector<Sweep> sw;
+        bs_plan_sweeps(pending, bs_vec_bits(s), sw);
+        pending.clear();
+        return bs_run_sweeps(s, sw);
+    };
+    const bool dm = s->kind == BS_KIND_DM;
+    for (int64_t i = 0; i < n_ops; i++) {
+        const bs_op& op = ops[i];
+        int rc = BS_OK;
+        if (op.kind == 2) continue;
+        if (op.kind == 0) {
+            rc = bs_lower_gate(s, op.matrix, op.n_targets, op.targets, op.n_controls, op.controls,
+                               op.control_values, op.flags, dm, pending);
+        } else if (op.kind == 1) {
+            if (!dm) return bs_fail(s, BS_ERR_STATE, "noise instruction on a state-vector simulator");
+            unsigned mode = (op.flags & BS_NOISE_PHYSICAL) ? BS_NOISE_PHYSICAL : noise_mode;
+            if (mode & BS_NOISE_PHYSICAL) {
+                rc = bs_lower_kraus_physical(s, op.matrix, op.n_matrices, op.n_targets, op.targets, op.flags, pending);
+            } else {
+                rc = flush();
+                if (!rc) rc = bs_kraus_reference(s, op.matrix, op.n_matrices, op.n_targets, op.targets, op.flags);
+            }
+        } else {
+            return bs_fail(s, BS_ERR_INVALID_ARG, "unknown op kind");
+        }
+        if (rc) return rc;
+    }
+    int rc = flush();
+    if (rc) return rc;
+    cudaEventRecord(s->ev1, s->stream);
+    rc = bs_cuda_check(s, cudaEventSynchronize(s->ev1), "evolve");
+    if (rc) return rc;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    s->stats.gpu_ms = ms;
+    return BS_OK;
+}
+
+}  // extern "C"

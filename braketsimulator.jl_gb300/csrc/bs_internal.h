@@ -1,0 +1,102 @@
+// Internal structures shared by the translation units of libbraket_gb300.so.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+#include "../../include/braket_gb300.h"
+
+#define BS_TILE_MAX_BITS 12      // 2^12 complex float-float values = 64 KiB of shared memory
+#define BS_TILE_LOW_BITS 5       // low endian bits always in a tile: 32 contiguous amplitudes
+#define BS_TILE_MAXK 4           // dense targets per tile gate (16x16 superoperators for 2q noise)
+
+// One gate inside a tile sweep.
+//   kind 0: dense 2^k x 2^k on tile-local bits tbit[0..k-1] (matrix bit j <-> tbit[j])
+//   kind 1: diagonal 2^k entries selected by global bits gbit[0..k-1]
+//   kind 2: monomial (one unit-modulus phase i^p per column) on tile-local bits
+// Controls: (tile_index & lc_mask) == lc_val for in-tile controls,
+//           (global_base & gc_mask) == gc_val for controls outside the tile.
+struct TileGate {
+    int32_t kind;
+    int32_t k;
+    int32_t tbit[BS_TILE_MAXK];
+    int32_t gbit[BS_MAX_TARGETS];
+    uint32_t lc_mask, lc_val;
+    uint64_t gc_mask, gc_val;
+    int32_t mat_off;            // offset (in cff units) into the sweep's matrix pool
+    int32_t perm_off;           // monomial: offset into the permutation pool (int32 pairs)
+};
+
+struct SweepDesc {
+    int32_t n_bits;             // endian bits of the vector (n for SV, 2n for DM)
+    int32_t T;                  // tile bits
+    int32_t L;                  // low contiguous bits
+    int32_t n_gates;
+    int32_t hi_bits[BS_TILE_MAX_BITS];
+    uint64_t tile_mask;
+    const TileGate* gates;      // device
+    const float4* mats;         // device, complex float-float entries (rh, rl, ih, il)
+    const int32_t* perms;       // device
+};
+
+struct HostGate {                // a gate after lowering to the canonical convention
+    int kind;                    // 0 dense, 1 diagonal, 2 monomial
+    int k;
+    int ebit[BS_MAX_TARGETS];    // endian bit of target j (matrix bit j)
+    std::vector<double> mat;     // interleaved complex; dense 4^k*2, diag 2^k*2
+    uint64_t cmask = 0, cval = 0;// controls on endian bits
+    std::vector<int> perm;       // monomial: column c -> (row, i-power)
+};
+
+struct Sweep {
+    std::vector<int> hi_bits;    // tile bits above the low contiguous block
+    std::vector<HostGate> gates;
+};
+
+struct bs_sim {
+    int kind = BS_KIND_SV;
+    int n = 0;                    // qubits
+    int precision = BS_PREC_C128;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void* state = nullptr;        // complex128: double2[len]
+    int64_t len = 0;              // elements of the state vector / vec(S)
+    int64_t cap_bytes = 0;
+    // scratch for reductions and sampling
+    void* scratch = nullptr;
+    int64_t scratch_bytes = 0;
+    double* alias_ap = nullptr;
+    int64_t* alias_ix = nullptr;
+    int64_t alias_len = 0;
+    bool alias_valid = false;
+    // plan upload buffer
+    void* plan_buf = nullptr;
+    int64_t plan_bytes = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bs_stats stats{};
+    std::string err;
+};
+
+// ---- helpers implemented in bs_api.cu
+int bs_fail(bs_sim* s, int code, const std::string& msg);
+int bs_cuda_check(bs_sim* s, cudaError_t e, const char* what);
+int bs_ensure_scratch(bs_sim* s, int64_t bytes);
+int bs_ensure_plan(bs_sim* s, int64_t bytes);
+int bs_vec_bits(const bs_sim* s);
+
+// ---- lowering (bs_plan.cpp)
+// Convert a gate (reference convention flags) into canonical HostGate(s) on the
+// vector's endian bits.  For DM, returns the column-side U and row-side conj(U).
+int bs_lower_gate(bs_sim* s, const double* matrix, int k, const int* targets, int nc,
+                  const int* controls, const int* cvals, unsigned flags, bool dm_superop,
+                  std::vector<HostGate>& out);
+int bs_lower_kraus_physical(bs_sim* s, const double* kraus, int nk, int k, const int* targets,
+                            unsigned flags, std::vector<HostGate>& out);
+void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, std::vector<Sweep>& out);
+
+// ---- execution (bs_tile.cu)
+int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps);
+
+// ---- reference-compat Kraus (bs_dm.cu)
+int bs_kraus_reference(bs_sim* s, const double* kraus, int nk, int k, const int* targets,
+                       unsigned flags);

@@ -1,0 +1,376 @@
+// Read-only reductions over the state: probabilities, Pauli-string and matrix
+// expectations, marginal probabilities.
+//
+// Reference: probabilities src/sv_simulator.jl:271 and src/dm_simulator.jl:262;
+// expectation src/sv_simulator.jl:240-248 (dot(psi, O psi) on a deep copy),
+// src/dm_simulator.jl:253-260 (trace of O applied to S);
+// marginal_probability src/result_types.jl:96-113.
+// The reference copies the whole state and re-sweeps it per observable factor;
+// here each Pauli term is one pair-read of the state and terms that flip the same
+// bits share the read.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <vector>
+#include "bs_internal.h"
+#include "bs_ff.cuh"
+
+namespace {
+
+constexpr int kRThreads = 256;
+constexpr int kMaxTermsPerPass = 8;
+
+__global__ void k_prob_sv(const double2* __restrict__ psi, double* __restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        cff x = load_c128(psi[i]);
+        ffacc a;
+        acc_first(a, x.rh, x.rl, x.rh, x.rl);
+        acc_add(a, x.ih, x.il, x.ih, x.il);
+        ff r = acc_done(a);
+        out[i] = ff2d(r.h, r.l);
+    }
+}
+
+__global__ void k_prob_dm(const double2* __restrict__ S, double* __restrict__ out, int64_t dim) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = S[i * (dim + 1)].x;
+}
+
+struct TermSet {
+    int nt;
+    uint64_t zm[kMaxTermsPerPass];
+    int ph[kMaxTermsPerPass];         // nY mod 4
+    int slot[kMaxTermsPerPass];       // output slot
+};
+
+// block reduction of per-thread doubles into partial[blockIdx.x * stride + slot]
+__device__ void block_sum_store(double v, double* partial, int64_t idx) {
+    __shared__ double red[kRThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = (l < (int)(blockDim.x >> 5)) ? red[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (l == 0) partial[idx] = v;
+    }
+}
+
+// SV Pauli terms sharing flip mask xm.  Pairs (i, i^xm) with the top bit of xm
+// clear contribute 2 Re(c(i) conj(psi_i) psi_{i^xm}); xm == 0 gives |psi_i|^2 * sign.
+__global__ void __launch_bounds__(kRThreads) k_pauli_sv(const double2* __restrict__ psi, int64_t n, uint64_t xm,
+                                                        TermSet ts, double* __restrict__ partial, int n_slots) {
+    ffsum acc[kMaxTermsPerPass];
+    for (int t = 0; t < kMaxTermsPerPass; t++) acc[t] = {0.f, 0.f};
+    const int64_t npairs = xm ? n / 2 : n;
+    int hb = xm ? 63 - __clzll((long long)xm) : 0;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npairs; p += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = p;
+        if (xm) { int64_t low = p & ((1LL << hb) - 1); i = ((p >> hb) << (hb + 1)) | low; }
+        cff a = load_c128(psi[i]);
+        float wrh, wrl, wih, wil;
+        if (xm) {
+            cff b = load_c128(psi[i ^ (int64_t)xm]);
+            ffacc r, m;
+            acc_first(r, a.rh, a.rl, b.rh, b.rl);
+            acc_add(r, a.ih, a.il, b.ih, b.il);
+            acc_first(m, a.rh, a.rl, b.ih, b.il);
+            acc_add(m, -a.ih, -a.il, b.rh, b.rl);
+            ff rr = acc_done(r), mm = acc_done(m);
+            wrh = 2.f * rr.h; wrl = 2.f * rr.l; wih = 2.f * mm.h; wil = 2.f * mm.l;
+        } else {
+            ffacc r;
+            acc_first(r, a.rh, a.rl, a.rh, a.rl);
+            acc_add(r, a.ih, a.il, a.ih, a.il);
+            ff rr = acc_done(r);
+            wrh = rr.h; wrl = rr.l; wih = 0.f; wil = 0.f;
+        }
+        for (int t = 0; t < ts.nt; t++) {
+            bool neg = __popcll((unsigned long long)i & ts.zm[t]) & 1;
+            float vh, vl;
+            switch (ts.ph[t]) {            // Re((-i)^ph * w)
+                case 0: vh = wrh; vl = wrl; break;
+                case 1: vh = wih; vl = wil; break;
+                case 2: vh = -wrh; vl = -wrl; break;
+                default: vh = -wih; vl = -wil; break;
+            }
+            if (neg) { vh = -vh; vl = -vl; }
+            fsum_add(acc[t], vh, vl);
+        }
+    }
+    for (int t = 0; t < ts.nt; t++)
+        block_sum_store(ff2d(acc[t].h, acc[t].l), partial, (int64_t)blockIdx.x * n_slots + ts.slot[t]);
+}
+
+// DM Pauli terms: E = sum_a Re(P[a, a^xm] S[a, a^xm]), S[r, c] at r + c*dim.
+__global__ void __launch_bounds__(kRThreads) k_pauli_dm(const double2* __restrict__ S, int64_t dim, uint64_t xm,
+                                                        TermSet ts, double* __restrict__ partial, int n_slots) {
+    ffsum acc[kMaxTermsPerPass];
+    for (int t = 0; t < kMaxTermsPerPass; t++) acc[t] = {0.f, 0.f};
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < dim; a += (int64_t)gridDim.x * blockDim.x) {
+        cff v = load_c128(S[a + (a ^ (int64_t)xm) * dim]);
+        for (int t = 0; t < ts.nt; t++) {
+            bool neg = __popcll((unsigned long long)a & ts.zm[t]) & 1;
+            float vh, vl;
+            switch (ts.ph[t]) {
+                case 0: vh = v.rh; vl = v.rl; break;
+                case 1: vh = v.ih; vl = v.il; break;
+                case 2: vh = -v.rh; vl = -v.rl; break;
+                default: vh = -v.ih; vl = -v.il; break;
+            }
+            if (neg) { vh = -vh; vl = -vl; }
+            fsum_add(acc[t], vh, vl);
+        }
+    }
+    for (int t = 0; t < ts.nt; t++)
+        block_sum_store(ff2d(acc[t].h, acc[t].l), partial, (int64_t)blockIdx.x * n_slots + ts.slot[t]);
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partial, int nblocks, int n_slots, double* __restrict__ out) {
+    // one block per slot; FP64 tree sum with a compensated leaf
+    int slot = blockIdx.x;
+    double s = 0.0, c = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        double y = partial[(int64_t)b * n_slots + slot] - c;
+        double t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) out[slot] = s;
+    }
+}
+
+__device__ __forceinline__ double2 cmulD(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// <O> for a k-target matrix (FP64): SV sum_g x^H O x, DM sum_g sum_ab O[a,b] S[(a,g),(b,g)]
+__global__ void __launch_bounds__(kRThreads) k_matrix_expect(const double2* __restrict__ st, int nbits_q, int k,
+                                                             const int* __restrict__ eb, const double2* __restrict__ O,
+                                                             int dm, double* __restrict__ partial) {
+    const int D = 1 << k;
+    const int64_t dim = (int64_t)1 << nbits_q;
+    const int64_t ngroups = dim >> k;
+    int ord[BS_MAX_TARGETS];
+    for (int q = 0; q < k; q++) ord[q] = eb[q];
+    for (int a = 0; a < k; a++)
+        for (int b = a + 1; b < k; b++)
+            if (ord[b] < ord[a]) { int t = ord[a]; ord[a] = ord[b]; ord[b] = t; }
+    double acc = 0.0;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < ngroups; g += (int64_t)gridDim.x * blockDim.x) {
+        int64_t p = g;
+        for (int q = 0; q < k; q++) {
+            int64_t low = p & ((1LL << ord[q]) - 1);
+            p = ((p >> ord[q]) << (ord[q] + 1)) | low;
+        }
+        for (int a = 0; a < D; a++) {
+            int64_t ia = p;
+            for (int q = 0; q < k; q++) if ((a >> q) & 1) ia |= 1LL << eb[q];
+            double2 xa = dm ? make_double2(0, 0) : st[ia];
+            for (int b = 0; b < D; b++) {
+                int64_t ib = p;
+                for (int q = 0; q < k; q++) if ((b >> q) & 1) ib |= 1LL << eb[q];
+                double2 o = O[a * D + b];
+                if (dm) {
+                    double2 v = cmulD(o, st[ia + ib * dim]);
+                    acc += v.x;
+                } else {
+                    double2 xb = st[ib];
+                    double2 v = cmulD(o, xb);          // O[a,b] x_b
+                    acc += xa.x * v.x + xa.y * v.y;    // Re(conj(x_a) * v)
+                }
+            }
+        }
+    }
+    block_sum_store(acc, partial, blockIdx.x);
+}
+
+// marginal probabilities: out[o] = sum of p_i over i whose target bits spell o
+// (output bit j <-> j-th smallest endian target bit)
+__global__ void __launch_bounds__(kRThreads) k_marginal(const double2* __restrict__ st, int dm, int nbits_q, int k,
+                                                        const int* __restrict__ eb_sorted, double* __restrict__ partial) {
+    extern __shared__ double hist[];
+    const int D = 1 << k;
+    const int64_t dim = (int64_t)1 << nbits_q;
+    for (int o = threadIdx.x; o < D; o += blockDim.x) hist[o] = 0.0;
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x) {
+        double p;
+        if (dm) {
+            p = st[i * (dim + 1)].x;
+        } else {
+            cff x = load_c128(st[i]);
+            ffacc a;
+            acc_first(a, x.rh, x.rl, x.rh, x.rl);
+            acc_add(a, x.ih, x.il, x.ih, x.il);
+            ff r = acc_done(a);
+            p = ff2d(r.h, r.l);
+        }
+        int o = 0;
+        for (int q = 0; q < k; q++) o |= (int)((i >> eb_sorted[q]) & 1) << q;
+        atomicAdd(&hist[o], p);
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < D; o += blockDim.x) partial[(int64_t)blockIdx.x * D + o] = hist[o];
+}
+
+int grid_for(int64_t work) {
+    int64_t b = (work + kRThreads - 1) / kRThreads;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 8));
+}
+
+}  // namespace
+
+extern "C" {
+
+int bs_probabilities(bs_sim* s, double* host_out, int64_t n) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    const int64_t dim = (int64_t)1 << s->n;
+    if (!host_out || n != dim) return bs_fail(s, BS_ERR_INVALID_ARG, "probability buffer length must be 2^n");
+    int rc = bs_ensure_scratch(s, dim * 8);
+    if (rc) return rc;
+    double* d = (double*)s->scratch;
+    if (s->kind == BS_KIND_SV) k_prob_sv<<<grid_for(dim), kRThreads, 0, s->stream>>>((const double2*)s->state, d, dim);
+    else k_prob_dm<<<grid_for(dim), kRThreads, 0, s->stream>>>((const double2*)s->state, d, dim);
+    rc = bs_cuda_check(s, cudaMemcpyAsync(host_out, d, (size_t)dim * 8, cudaMemcpyDeviceToHost, s->stream), "probabilities");
+    if (rc) return rc;
+    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "probabilities sync");
+}
+
+int bs_expectation_pauli(bs_sim* s, int n_terms, const uint64_t* xmask, const uint64_t* zmask, const double* coeffs,
+                         double* out) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (n_terms < 0 || (n_terms > 0 && (!xmask || !zmask || !out))) return bs_fail(s, BS_ERR_INVALID_ARG, "bad term arrays");
+    if (n_terms == 0) return BS_OK;
+    const int n = s->n;
+    const uint64_t qmask = (n >= 64) ? ~0ULL : ((1ULL << n) - 1);
+    // group by flip mask on endian bits
+    std::map<uint64_t, std::vector<int>> groups;
+    std::vector<uint64_t> zme(n_terms);
+    std::vector<int> ph(n_terms);
+    for (int t = 0; t < n_terms; t++) {
+        if ((xmask[t] | zmask[t]) & ~qmask) return bs_fail(s, BS_ERR_INVALID_ARG, "Pauli mask names a qubit outside the register");
+        uint64_t xe = 0, ze = 0;
+        int ny = 0;
+        for (int q = 0; q < n; q++) {
+            bool x = (xmask[t] >> q) & 1ULL, z = (zmask[t] >> q) & 1ULL;
+            if (x) xe |= 1ULL << (n - 1 - q);
+            if (z) ze |= 1ULL << (n - 1 - q);
+            if (x && z) ny++;
+        }
+        zme[t] = ze;
+        ph[t] = ny & 3;
+        groups[xe].push_back(t);
+    }
+    const int64_t dim = (int64_t)1 << n;
+    const int64_t work = (s->kind == BS_KIND_SV) ? dim : dim;
+    const int nb = grid_for(work);
+    int rc = bs_ensure_scratch(s, ((int64_t)nb * n_terms + n_terms) * 8);
+    if (rc) return rc;
+    double* partial = (double*)s->scratch;
+    double* res = partial + (int64_t)nb * n_terms;
+    rc = bs_cuda_check(s, cudaMemsetAsync(partial, 0, (size_t)nb * n_terms * 8, s->stream), "clear partials");
+    if (rc) return rc;
+    for (auto& kv : groups) {
+        const std::vector<int>& ts = kv.second;
+        for (size_t c0 = 0; c0 < ts.size(); c0 += kMaxTermsPerPass) {
+            TermSet set{};
+            set.nt = (int)std::min<size_t>(kMaxTermsPerPass, ts.size() - c0);
+            for (int j = 0; j < set.nt; j++) {
+                int t = ts[c0 + (size_t)j];
+                set.zm[j] = zme[t];
+                set.ph[j] = ph[t];
+                set.slot[j] = t;
+            }
+            if (s->kind == BS_KIND_SV)
+                k_pauli_sv<<<nb, kRThreads, 0, s->stream>>>((const double2*)s->state, dim, kv.first, set, partial, n_terms);
+            else
+                k_pauli_dm<<<nb, kRThreads, 0, s->stream>>>((const double2*)s->state, dim, kv.first, set, partial, n_terms);
+        }
+    }
+    k_sum_partials<<<n_terms, 256, 0, s->stream>>>(partial, nb, n_terms, res);
+    rc = bs_cuda_check(s, cudaMemcpyAsync(out, res, (size_t)n_terms * 8, cudaMemcpyDeviceToHost, s->stream), "expectation");
+    if (rc) return rc;
+    rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "expectation sync");
+    if (rc) return rc;
+    if (coeffs)
+        for (int t = 0; t < n_terms; t++) out[t] *= coeffs[t];
+    return BS_OK;
+}
+
+int bs_expectation_matrix(bs_sim* s, const double* matrix, int k, const int* targets, unsigned flags, double* out) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (!matrix || !targets || !out || k < 1 || k > BS_MAX_TARGETS) return bs_fail(s, BS_ERR_INVALID_ARG, "bad observable");
+    uint64_t seen = 0;
+    for (int i = 0; i < k; i++) {
+        if (targets[i] < 0 || targets[i] >= s->n) return bs_fail(s, BS_ERR_INVALID_ARG, "target qubit out of range");
+        if ((seen >> targets[i]) & 1ULL) return bs_fail(s, BS_ERR_INVALID_ARG, "repeated qubit");
+        seen |= 1ULL << targets[i];
+    }
+    std::vector<int> ct(targets, targets + k);
+    if (flags & BS_GATE_SORTED_TARGETS) std::sort(ct.begin(), ct.end(), [](int a, int b) { return a > b; });
+    else if (flags & BS_GATE_MSB_FIRST) std::reverse(ct.begin(), ct.end());
+    std::vector<int> eb(k);
+    for (int j = 0; j < k; j++) eb[j] = s->n - 1 - ct[j];
+    const int D = 1 << k;
+    const int64_t dim = (int64_t)1 << s->n;
+    const int nb = grid_for(dim >> k);
+    const int64_t mbytes = (int64_t)D * D * 16;
+    int rc = bs_ensure_plan(s, 256 + mbytes);
+    if (rc) return rc;
+    rc = bs_ensure_scratch(s, ((int64_t)nb + 1) * 8);
+    if (rc) return rc;
+    std::vector<char> host((size_t)(256 + mbytes), 0);
+    std::memcpy(host.data(), eb.data(), sizeof(int) * (size_t)k);
+    std::memcpy(host.data() + 256, matrix, (size_t)mbytes);
+    rc = bs_cuda_check(s, cudaMemcpyAsync(s->plan_buf, host.data(), host.size(), cudaMemcpyHostToDevice, s->stream), "observable upload");
+    if (rc) return rc;
+    double* partial = (double*)s->scratch;
+    k_matrix_expect<<<nb, kRThreads, 0, s->stream>>>((const double2*)s->state, s->n, k, (const int*)s->plan_buf,
+                                                      (const double2*)((char*)s->plan_buf + 256), s->kind == BS_KIND_DM, partial);
+    k_sum_partials<<<1, 256, 0, s->stream>>>(partial, nb, 1, partial + nb);
+    rc = bs_cuda_check(s, cudaMemcpyAsync(out, partial + nb, 8, cudaMemcpyDeviceToHost, s->stream), "expectation");
+    if (rc) return rc;
+    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "expectation sync");
+}
+
+int bs_marginal_probabilities(bs_sim* s, int k, const int* targets, double* host_out) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (!targets || !host_out || k < 1 || k > 12 || k > s->n) return bs_fail(s, BS_ERR_INVALID_ARG, "marginal needs 1..12 targets");
+    uint64_t seen = 0;
+    for (int i = 0; i < k; i++) {
+        if (targets[i] < 0 || targets[i] >= s->n) return bs_fail(s, BS_ERR_INVALID_ARG, "target qubit out of range");
+        if ((seen >> targets[i]) & 1ULL) return bs_fail(s, BS_ERR_INVALID_ARG, "repeated qubit");
+        seen |= 1ULL << targets[i];
+    }
+    std::vector<int> eb(k);
+    for (int j = 0; j < k; j++) eb[j] = s->n - 1 - targets[j];
+    std::sort(eb.begin(), eb.end());
+    const int D = 1 << k;
+    const int64_t dim = (int64_t)1 << s->n;
+    const int nb = grid_for(dim);
+    int rc = bs_ensure_plan(s, 256);
+    if (rc) return rc;
+    rc = bs_ensure_scratch(s, ((int64_t)nb * D + D) * 8);
+    if (rc) return rc;
+    rc = bs_cuda_check(s, cudaMemcpyAsync(s->plan_buf, eb.data(), sizeof(int) * (size_t)k, cudaMemcpyHostToDevice, s->stream), "marginal upload");
+    if (rc) return rc;
+    double* partial = (double*)s->scratch;
+    k_marginal<<<nb, kRThreads, (size_t)D * 8, s->stream>>>((const double2*)s->state, s->kind == BS_KIND_DM, s->n, k,
+                                                             (const int*)s->plan_buf, partial);
+    k_sum_partials<<<D, 256, 0, s->stream>>>(partial, nb, D, partial + (int64_t)nb * D);
+    rc = bs_cuda_check(s, cudaMemcpyAsync(host_out, partial + (int64_t)nb * D, (size_t)D * 8, cudaMemcpyDeviceToHost, s->stream), "marginal");
+    if (rc) return rc;
+    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "marginal sync");
+}
+
+}  // extern "C"

@@ -1,0 +1,398 @@
+// Tile sweeps: one CTA owns 2^T amplitudes of the state (the L lowest endian bits
+// plus T-L chosen higher bits, all other bits fixed by the CTA index), converts
+// them once to float-float in shared memory, applies every gate of the sweep
+// whose targets lie inside the tile, and writes them back.  A sweep therefore
+// reads and writes the state once however many gates it carries.
+//
+// Reference kernels replaced (src/gate_kernels.jl): 1q :489-537, 2q :540-576,
+// controlled :579-670, generic k-target :753-775, custom diagonal/excitation
+// kernels src/custom_gates.jl:364-416; the density-matrix gate of
+// src/dm_simulator.jl:130-140 is two tile gates (column bits U, row bits conj U).
+#include <algorithm>
+#include <cstring>
+#include "bs_internal.h"
+#include "bs_ff.cuh"
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ int insert0(int x, int bit) {
+    int low = x & ((1 << bit) - 1);
+    return ((x >> bit) << (bit + 1)) | low;
+}
+__device__ __forceinline__ cff f4c(float4 v) { return {v.x, v.y, v.z, v.w}; }
+__device__ __forceinline__ float4 c4f(const cff& c) { return make_float4(c.rh, c.rl, c.ih, c.il); }
+
+template <int K>
+__device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* __restrict__ mats) {
+    constexpr int D = 1 << K;
+    int pos[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) pos[q] = g.tbit[q];
+    // ascending order for padding
+#pragma unroll
+    for (int a = 0; a < K; a++)
+#pragma unroll
+        for (int b = a + 1; b < K; b++)
+            if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
+    const int ngroups = 1 << (T - K);
+    const float4* m = mats + g.mat_off;
+    for (int gr = threadIdx.x; gr < ngroups; gr += blockDim.x) {
+        int jb = gr;
+#pragma unroll
+        for (int q = 0; q < K; q++) jb = insert0(jb, pos[q]);
+        if ((jb & (int)g.lc_mask) != (int)g.lc_val) continue;
+        cff x[D];
+        int idx[D];
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+            int j = jb;
+#pragma unroll
+            for (int q = 0; q < K; q++) if ((c >> q) & 1) j |= 1 << g.tbit[q];
+            idx[c] = j;
+            x[c] = f4c(sm[j]);
+        }
+#pragma unroll
+        for (int r = 0; r < D; r++) {
+            ffacc ar, ai;
+            cmac_first(ar, ai, f4c(__ldg(m + r * D)), x[0]);
+#pragma unroll
+            for (int c = 1; c < D; c++) cmac(ar, ai, f4c(__ldg(m + r * D + c)), x[c]);
+            sm[idx[r]] = c4f(cdone(ar, ai));
+        }
+    }
+}
+
+// monomial gate: column c goes to row perm[2c] with phase i^perm[2c+1]
+template <int K>
+__device__ void tile_monomial(float4* sm, int T, const TileGate& g, const int32_t* __restrict__ perms) {
+    constexpr int D = 1 << K;
+    int pos[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) pos[q] = g.tbit[q];
+#pragma unroll
+    for (int a = 0; a < K; a++)
+#pragma unroll
+        for (int b = a + 1; b < K; b++)
+            if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
+    const int ngroups = 1 << (T - K);
+    const int32_t* p = perms + g.perm_off;
+    for (int gr = threadIdx.x; gr < ngroups; gr += blockDim.x) {
+        int jb = gr;
+#pragma unroll
+        for (int q = 0; q < K; q++) jb = insert0(jb, pos[q]);
+        if ((jb & (int)g.lc_mask) != (int)g.lc_val) continue;
+        float4 x[D];
+        int idx[D];
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+            int j = jb;
+#pragma unroll
+            for (int q = 0; q < K; q++) if ((c >> q) & 1) j |= 1 << g.tbit[q];
+            idx[c] = j;
+            x[c] = sm[j];
+        }
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+            int r = __ldg(p + 2 * c), ph = __ldg(p + 2 * c + 1);
+            sm[idx[r]] = c4f(cmul_ipow(f4c(x[c]), ph));
+        }
+    }
+}
+
+__device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const float4* __restrict__ mats,
+                          int64_t base, const int64_t* off_tab) {
+    const int nt = 1 << T, lowmask = (1 << L) - 1;
+    const float4* m = mats + g.mat_off;
+    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        if ((j & (int)g.lc_mask) != (int)g.lc_val) continue;
+        int64_t gi = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+        int di = 0;
+        for (int q = 0; q < g.k; q++) di |= (int)((gi >> g.gbit[q]) & 1) << q;
+        float4 d = __ldg(m + di);
+        if (d.y == 0.f && d.w == 0.f) {
+            if (d.z == 0.f && d.x == 1.f) continue;
+            if (d.z == 0.f && d.x == -1.f) { sm[j] = c4f(cmul_ipow(f4c(sm[j]), 2)); continue; }
+            if (d.x == 0.f && d.z == 1.f) { sm[j] = c4f(cmul_ipow(f4c(sm[j]), 1)); continue; }
+            if (d.x == 0.f && d.z == -1.f) { sm[j] = c4f(cmul_ipow(f4c(sm[j]), 3)); continue; }
+        }
+        sm[j] = c4f(cmul(f4c(d), f4c(sm[j])));
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_tile_sweep(double2* __restrict__ psi, SweepDesc d, int64_t tile0) {
+    extern __shared__ float4 smem[];
+    const int T = d.T, L = d.L, H = T - L;
+    const int nt = 1 << T;
+    int64_t* off_tab = reinterpret_cast<int64_t*>(smem + nt);
+    __shared__ int64_t s_base;
+    const int64_t tile = tile0 + (int64_t)blockIdx.x;
+    if (threadIdx.x == 0) {
+        int64_t base = 0;
+        int src = 0;
+        for (int bit = 0; bit < d.n_bits; bit++)
+            if (!((d.tile_mask >> bit) & 1ULL)) { base |= ((tile >> src) & 1LL) << bit; src++; }
+        s_base = base;
+    }
+    for (int i = threadIdx.x; i < (1 << H); i += blockDim.x) {
+        int64_t o = 0;
+        for (int j = 0; j < H; j++) if ((i >> j) & 1) o |= 1LL << d.hi_bits[j];
+        off_tab[i] = o;
+    }
+    __syncthreads();
+    const int64_t base = s_base;
+    const int lowmask = (1 << L) - 1;
+    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+        smem[j] = c4f(load_c128(__ldcs(psi + gidx)));
+    }
+    __syncthreads();
+    for (int gi = 0; gi < d.n_gates; gi++) {
+        const TileGate g = d.gates[gi];
+        if ((base & (int64_t)g.gc_mask) != (int64_t)g.gc_val) continue;   // uniform in the CTA
+        if (g.kind == 1) {
+            tile_diag(smem, T, L, g, d.mats, base, off_tab);
+        } else if (g.kind == 0) {
+            switch (g.k) {
+                case 1: tile_dense<1>(smem, T, g, d.mats); break;
+                case 2: tile_dense<2>(smem, T, g, d.mats); break;
+                case 3: tile_dense<3>(smem, T, g, d.mats); break;
+                default: tile_dense<4>(smem, T, g, d.mats); break;
+            }
+        } else {
+            switch (g.k) {
+                case 1: tile_monomial<1>(smem, T, g, d.perms); break;
+                case 2: tile_monomial<2>(smem, T, g, d.perms); break;
+                case 3: tile_monomial<3>(smem, T, g, d.perms); break;
+                default: tile_monomial<4>(smem, T, g, d.perms); break;
+            }
+        }
+        __syncthreads();
+    }
+    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+        __stcs(psi + gidx, store_c128(f4c(smem[j])));
+    }
+}
+
+// Dense gate with more targets than a tile holds: one CTA per group of 2^k
+// amplitudes, gathered into shared memory, rows computed by the CTA's threads.
+__global__ void __launch_bounds__(kThreads) k_dense_big(double2* __restrict__ psi, int n_bits, int k,
+                                                        const int* __restrict__ ebits, uint64_t cmask,
+                                                        uint64_t cval, const float4* __restrict__ mat,
+                                                        int64_t group0) {
+    extern __shared__ float4 smem[];
+    const int D = 1 << k;
+    __shared__ int64_t s_base;
+    __shared__ int s_skip;
+    if (threadIdx.x == 0) {
+        // insert zeros at the sorted target bits
+        int ord[BS_MAX_TARGETS];
+        for (int q = 0; q < k; q++) ord[q] = ebits[q];
+        for (int a = 0; a < k; a++)
+            for (int b = a + 1; b < k; b++)
+                if (ord[b] < ord[a]) { int t = ord[a]; ord[a] = ord[b]; ord[b] = t; }
+        int64_t x = group0 + (int64_t)blockIdx.x;
+        for (int q = 0; q < k; q++) {
+            int64_t low = x & ((1LL << ord[q]) - 1);
+            x = ((x >> ord[q]) << (ord[q] + 1)) | low;
+        }
+        s_base = x;
+        s_skip = ((uint64_t)x & cmask) != cval;
+    }
+    __syncthreads();
+    if (s_skip) return;
+    const int64_t base = s_base;
+    for (int c = threadIdx.x; c < D; c += blockDim.x) {
+        int64_t gi = base;
+        for (int q = 0; q < k; q++) if ((c >> q) & 1) gi |= 1LL << ebits[q];
+        smem[c] = c4f(load_c128(psi[gi]));
+    }
+    __syncthreads();
+    float4* outv = smem + D;
+    for (int r = threadIdx.x; r < D; r += blockDim.x) {
+        ffacc ar, ai;
+        cmac_first(ar, ai, f4c(mat[(int64_t)r * D]), f4c(smem[0]));
+        for (int c = 1; c < D; c++) cmac(ar, ai, f4c(mat[(int64_t)r * D + c]), f4c(smem[c]));
+        outv[r] = c4f(cdone(ar, ai));
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < D; r += blockDim.x) {
+        int64_t gi = base;
+        for (int q = 0; q < k; q++) if ((r >> q) & 1) gi |= 1LL << ebits[q];
+        psi[gi] = store_c128(f4c(outv[r]));
+    }
+}
+
+inline void split_d(double x, float& h, float& l) {
+    h = (float)x;
+    l = (float)(x - (double)h);
+}
+inline float4 to_cff(double re, double im) {
+    float4 v;
+    split_d(re, v.x, v.y);
+    split_d(im, v.z, v.w);
+    return v;
+}
+
+}  // namespace
+
+int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
+    if (sweeps.empty()) return BS_OK;
+    const int n_bits = bs_vec_bits(s);
+    const int T = std::min(BS_TILE_MAX_BITS, n_bits);
+    const int L = std::min(BS_TILE_LOW_BITS, T);
+    // pack: per sweep [TileGate...], then one float4 pool, then one int pool
+    std::vector<TileGate> tg;
+    std::vector<float4> mats;
+    std::vector<int32_t> perms;
+    struct Launch { int64_t gate0; int n_gates; std::vector<int> hi; bool big; int big_gate; };
+    std::vector<Launch> launches;
+    std::vector<int32_t> big_bits;
+    for (const Sweep& sw : sweeps) {
+        Launch ln;
+        ln.gate0 = (int64_t)tg.size();
+        ln.n_gates = 0;
+        ln.hi = sw.hi_bits;
+        ln.big = false;
+        ln.big_gate = -1;
+        // tile-local position of each endian bit
+        int local[64];
+        for (int b = 0; b < 64; b++) local[b] = -1;
+        for (int b = 0; b < L; b++) local[b] = b;
+        for (size_t i = 0; i < sw.hi_bits.size(); i++) local[sw.hi_bits[i]] = L + (int)i;
+        for (const HostGate& hg : sw.gates) {
+            bool big = hg.kind != 1 && hg.k > BS_TILE_MAXK;
+            if (!big && hg.kind != 1)
+                for (int q = 0; q < hg.k; q++) if (local[hg.ebit[q]] < 0) big = true;
+            if (big) {
+                // runs alone: sweeps hold a single out-of-tile gate
+                ln.big = true;
+                ln.big_gate = (int)tg.size();
+                TileGate t{};
+                t.kind = hg.kind;
+                t.k = hg.k;
+                t.gc_mask = hg.cmask;
+                t.gc_val = hg.cval;
+                t.mat_off = (int32_t)mats.size();
+                t.perm_off = (int32_t)big_bits.size();
+                for (int q = 0; q < hg.k; q++) big_bits.push_back(hg.ebit[q]);
+                if (hg.kind == 0) {
+                    for (int i = 0; i < (1 << (2 * hg.k)); i++) mats.push_back(to_cff(hg.mat[2 * i], hg.mat[2 * i + 1]));
+                } else {
+                    // monomial given as dense
+                    int D = 1 << hg.k;
+                    std::vector<float4> dense((size_t)D * D, make_float4(0, 0, 0, 0));
+                    for (int c = 0; c < D; c++) {
+                        int r = hg.perm[2 * c], p = hg.perm[2 * c + 1] & 3;
+                        double re = (p == 0) ? 1 : (p == 2 ? -1 : 0), im = (p == 1) ? 1 : (p == 3 ? -1 : 0);
+                        dense[(size_t)r * D + c] = to_cff(re, im);
+                    }
+                    t.kind = 0;
+                    mats.insert(mats.end(), dense.begin(), dense.end());
+                }
+                tg.push_back(t);
+                ln.n_gates++;
+                continue;
+            }
+            TileGate t{};
+            t.kind = hg.kind;
+            t.k = hg.k;
+            uint64_t gcm = 0, gcv = 0;
+            uint32_t lcm = 0, lcv = 0;
+            for (int b = 0; b < n_bits; b++) {
+                if (!((hg.cmask >> b) & 1ULL)) continue;
+                uint64_t v = (hg.cval >> b) & 1ULL;
+                if (local[b] >= 0) { lcm |= 1u << local[b]; lcv |= (uint32_t)v << local[b]; }
+                else { gcm |= 1ULL << b; gcv |= v << b; }
+            }
+            t.lc_mask = lcm; t.lc_val = lcv; t.gc_mask = gcm; t.gc_val = gcv;
+            for (int q = 0; q < hg.k; q++) {
+                t.gbit[q] = hg.ebit[q];
+                if (q < BS_TILE_MAXK) t.tbit[q] = local[hg.ebit[q]];
+            }
+            t.mat_off = (int32_t)mats.size();
+            t.perm_off = (int32_t)perms.size();
+            if (hg.kind == 0) {
+                for (int i = 0; i < (1 << (2 * hg.k)); i++) mats.push_back(to_cff(hg.mat[2 * i], hg.mat[2 * i + 1]));
+            } else if (hg.kind == 1) {
+                for (int i = 0; i < (1 << hg.k); i++) mats.push_back(to_cff(hg.mat[2 * i], hg.mat[2 * i + 1]));
+            } else {
+                perms.insert(perms.end(), hg.perm.begin(), hg.perm.end());
+            }
+            tg.push_back(t);
+            ln.n_gates++;
+        }
+        launches.push_back(std::move(ln));
+    }
+    // upload
+    auto al = [](int64_t x) { return (x + 255) & ~(int64_t)255; };
+    int64_t b_tg = al((int64_t)tg.size() * (int64_t)sizeof(TileGate));
+    int64_t b_m = al((int64_t)mats.size() * (int64_t)sizeof(float4));
+    int64_t b_p = al((int64_t)(perms.size() + big_bits.size() + 1) * (int64_t)sizeof(int32_t));
+    int rc = bs_ensure_plan(s, b_tg + b_m + b_p);
+    if (rc) return rc;
+    std::vector<char> host((size_t)(b_tg + b_m + b_p), 0);
+    if (!tg.empty()) std::memcpy(host.data(), tg.data(), tg.size() * sizeof(TileGate));
+    if (!mats.empty()) std::memcpy(host.data() + b_tg, mats.data(), mats.size() * sizeof(float4));
+    if (!perms.empty()) std::memcpy(host.data() + b_tg + b_m, perms.data(), perms.size() * sizeof(int32_t));
+    if (!big_bits.empty())
+        std::memcpy(host.data() + b_tg + b_m + perms.size() * sizeof(int32_t), big_bits.data(), big_bits.size() * sizeof(int32_t));
+    char* dev = (char*)s->plan_buf;
+    rc = bs_cuda_check(s, cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, s->stream), "plan upload");
+    if (rc) return rc;
+    const TileGate* d_tg = (const TileGate*)dev;
+    const float4* d_m = (const float4*)(dev + b_tg);
+    const int32_t* d_p = (const int32_t*)(dev + b_tg + b_m);
+    const int32_t* d_big = d_p + perms.size();
+
+    const int H = T - L;
+    const size_t smem = ((size_t)1 << T) * sizeof(float4) + ((size_t)1 << H) * sizeof(int64_t);
+    static bool attr_set[64] = {false};
+    if (!attr_set[s->device & 63]) {
+        cudaFuncSetAttribute(k_tile_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        cudaFuncSetAttribute(k_dense_big, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        attr_set[s->device & 63] = true;
+    }
+    double2* psi = (double2*)s->state;
+    const int64_t ntiles = (int64_t)1 << (n_bits - T);
+    for (const Launch& ln : launches) {
+        if (ln.big) {
+            const TileGate& t = tg[(size_t)ln.big_gate];
+            int64_t groups = (int64_t)1 << (n_bits - t.k);
+            size_t bsm = ((size_t)2 << t.k) * sizeof(float4);
+            if (bsm > 100 * 1024) return bs_fail(s, BS_ERR_UNSUPPORTED, "gate has too many targets");
+            for (int64_t g0 = 0; g0 < groups; g0 += 1LL << 30) {
+                int64_t ng = std::min<int64_t>(groups - g0, 1LL << 30);
+                k_dense_big<<<(unsigned)ng, kThreads, bsm, s->stream>>>(psi, n_bits, t.k, d_big + t.perm_off,
+                                                                        t.gc_mask, t.gc_val, d_m + t.mat_off, g0);
+            }
+            s->stats.kernel_launches++;
+            s->stats.sweeps++;
+            s->stats.gates++;
+            s->stats.bytes_moved += 32.0 * (double)s->len;
+            continue;
+        }
+        SweepDesc d{};
+        d.n_bits = n_bits;
+        d.T = T;
+        d.L = L;
+        d.n_gates = ln.n_gates;
+        uint64_t tm = (L >= 64) ? ~0ULL : ((1ULL << L) - 1);
+        for (int i = 0; i < H; i++) { d.hi_bits[i] = ln.hi[(size_t)i]; tm |= 1ULL << ln.hi[(size_t)i]; }
+        d.tile_mask = tm;
+        d.gates = d_tg + ln.gate0;
+        d.mats = d_m;
+        d.perms = d_p;
+        for (int64_t t0 = 0; t0 < ntiles; t0 += (1LL << 30)) {
+            int64_t nb = std::min<int64_t>(ntiles - t0, 1LL << 30);
+            k_tile_sweep<<<(unsigned)nb, kThreads, smem, s->stream>>>(psi, d, t0);
+        }
+        s->stats.kernel_launches++;
+        s->stats.sweeps++;
+        s->stats.gates += ln.n_gates;
+        s->stats.bytes_moved += 32.0 * (double)s->len;
+    }
+    return bs_cuda_check(s, cudaGetLastError(), "tile sweep launch");
+}

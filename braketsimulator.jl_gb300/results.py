@@ -1,0 +1,198 @@
+"""Result types and ``calculate`` (src/result_types.jl:82-246, src/results.jl)."""
+from __future__ import annotations
+
+import itertools
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .observables import HermitianObservable, I, Observable, StandardObservable, TensorProduct
+from .simulators import DensityMatrixSimulator, StateVectorSimulator
+
+
+@dataclass
+class StateVector:
+    pass
+
+
+@dataclass
+class Amplitude:
+    states: list
+
+
+@dataclass
+class Probability:
+    targets: tuple = ()
+
+
+@dataclass
+class DensityMatrix:
+    targets: tuple = ()
+
+
+@dataclass
+class Expectation:
+    observable: Observable
+    targets: tuple = ()
+
+
+@dataclass
+class Variance:
+    observable: Observable
+    targets: tuple = ()
+
+
+@dataclass
+class Sample:
+    observable: Observable
+    targets: tuple = ()
+
+
+def marginal_probability(probs: np.ndarray, qubit_count: int, targets) -> np.ndarray:
+    """src/result_types.jl:96-113 on a host vector: output bit j <-> j-th smallest endian target."""
+    targets = list(targets)
+    p = np.asarray(probs, dtype=np.float64).reshape([2] * qubit_count) if qubit_count else np.asarray(probs)
+    unused = [q for q in range(qubit_count) if q not in targets]
+    # axis a of the reshaped array is qubit a (C order: qubit 0 = most significant)
+    m = p.sum(axis=tuple(unused)) if unused else p
+    kept = sorted(targets)
+    return np.ascontiguousarray(m).reshape(-1) if kept else np.array([float(np.sum(p))])
+
+
+def permute_probability(probs: np.ndarray, qubit_count: int, targets) -> np.ndarray:
+    """src/result_types.jl:115-127."""
+    t = list(targets)
+    out = np.zeros(1 << len(t))
+    for ix in range(1 << len(t)):
+        bits = [(ix >> q) & 1 for q in range(qubit_count)]
+        perm = [bits[qubit_count - tt - 1] for tt in t]
+        new = sum(b << q for q, b in zip(range(qubit_count), perm))
+        out[new] = probs[ix]
+    return out
+
+
+def permute_density_matrix(rho: np.ndarray, qubit_count: int, targets) -> np.ndarray:
+    """src/result_types.jl:129-149."""
+    t = list(targets)
+    d = 1 << len(t)
+
+    def idx(ix):
+        bits = [(ix >> q) & 1 for q in range(qubit_count)]
+        perm = [bits[qubit_count - tt - 1] for tt in t]
+        return sum(b << q for q, b in zip(range(qubit_count), perm))
+
+    out = np.zeros((d, d), dtype=rho.dtype)
+    for ix in range(d):
+        for jx in range(d):
+            out[idx(ix), idx(jx)] = rho[ix, jx]
+    return out
+
+
+def _swap_bits(ix, mapping):
+    for a, b in mapping.items():
+        if a < b and ((ix >> a) & 1) != ((ix >> b) & 1):
+            ix ^= (1 << a) | (1 << b)
+    return ix
+
+
+def partial_trace(state, output_qubits=None):
+    """Reduced density matrix (src/sv_simulator.jl:273-318 for a vector,
+    src/dm_simulator.jl:280-323 for a matrix)."""
+    state = np.asarray(state, dtype=np.complex128)
+    vec = state.ndim == 1
+    n = int(round(np.log2(state.shape[0])))
+    if output_qubits is None:
+        output_qubits = list(range(n))
+    output_qubits = list(output_qubits)
+    if not output_qubits:
+        return np.sum(np.abs(state) ** 2) if vec else np.trace(state)
+    if len(set(output_qubits)) == n:
+        return np.outer(state, state.conj()) if vec else state
+    traced = [q for q in range(n) if q not in output_qubits]
+    endian = sorted(n - q - 1 for q in traced)
+    combos = [()] + [c for r in range(1, len(endian) + 1) for c in itertools.combinations(endian, r)]
+    dim = 1 << (n - len(traced))
+    out = np.zeros((dim, dim), dtype=np.complex128)
+    needs_perm = output_qubits != sorted(output_qubits)
+    fn = len(output_qubits)
+    mapping = dict(zip([fn - q - 1 for q in output_qubits], [fn - q - 1 for q in range(fn)])) if needs_perm else {}
+
+    def pad(ix):
+        for b in endian:
+            low = ix & ((1 << b) - 1)
+            ix = ((ix >> b) << (b + 1)) | low
+        return ix
+
+    for ix in range(dim):
+        for jx in range(dim if not vec else dim):
+            if vec and jx < ix:
+                continue
+            pi, pj = pad(ix), pad(jx)
+            fi = [pi ^ sum(1 << b for b in c) for c in combos]
+            fj = [pj ^ sum(1 << b for b in c) for c in combos]
+            oi = _swap_bits(ix, mapping) if needs_perm else ix
+            oj = _swap_bits(jx, mapping) if needs_perm else jx
+            if vec:
+                tr = np.vdot(state[fj], state[fi])
+                out[oi, oj] += tr
+                if oj != oi:
+                    out[oj, oi] += np.conj(tr)
+            else:
+                out[oi, oj] = np.sum(state[fi, fj])
+    return out
+
+
+def _targets(rt, sim):
+    t = tuple(rt.targets) if rt.targets is not None else ()
+    return t if t else tuple(range(sim.qubit_count))
+
+
+def _op_squared(sim, obs, targets):
+    """expectation_op_squared (src/result_types.jl:168-194)."""
+    if isinstance(obs, (StandardObservable, I)):
+        return 1.0
+    if isinstance(obs, TensorProduct):
+        if all(isinstance(f, (StandardObservable, I)) for f in obs.factors):
+            return 1.0
+        sq = [I() if isinstance(f, (StandardObservable, I)) else HermitianObservable(f.matrix @ f.matrix) for f in obs.factors]
+        return sim.expectation(TensorProduct(sq), *targets)
+    return sim.expectation(HermitianObservable(obs.matrix @ obs.matrix), *targets)
+
+
+def calculate(rt, sim):
+    """calculate (src/result_types.jl:82-246)."""
+    n = sim.qubit_count
+    if isinstance(rt, StateVector):
+        return sim.state_vector.copy()
+    if isinstance(rt, Amplitude):
+        sv = sim.state_vector
+        return {s: sv[int(s, 2)] for s in rt.states}
+    if isinstance(rt, Probability):
+        t = tuple(rt.targets or ())
+        if not t or list(t) == list(range(n)):
+            return sim.probabilities()
+        if len(t) == n:
+            return permute_probability(sim.probabilities(), n, list(t))
+        if len(t) <= 12:
+            return sim.marginal_probabilities(sorted(t))
+        return marginal_probability(sim.probabilities(), n, t)
+    if isinstance(rt, Expectation):
+        t = _targets(rt, sim)
+        if len(t) == rt.observable.qubit_count():
+            return sim.expectation(rt.observable, *t)
+        return [sim.expectation(rt.observable, q) for q in t]
+    if isinstance(rt, Variance):
+        t = _targets(rt, sim)
+        if len(t) == rt.observable.qubit_count():
+            return _op_squared(sim, rt.observable, t) - sim.expectation(rt.observable, *t) ** 2
+        return [_op_squared(sim, rt.observable, (q,)) - sim.expectation(rt.observable, q) ** 2 for q in t]
+    if isinstance(rt, DensityMatrix):
+        t = tuple(rt.targets or ())
+        full = isinstance(sim, DensityMatrixSimulator)
+        rho = sim.density_matrix if full else None
+        if not t or list(t) == list(range(n)):
+            return rho if full else sim.density_matrix()
+        if len(t) == n:
+            return permute_density_matrix(rho if full else sim.density_matrix(), n, list(t))
+        return partial_trace(rho if full else sim.state_vector, list(t))
+    raise TypeError(f"unsupported result type {rt!r}")

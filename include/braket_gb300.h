@@ -1,0 +1,176 @@
+/*
+ * braket_gb300.h — C ABI of the GB300 state-vector / density-matrix engine.
+ *
+ * One handle (bs_sim) owns one quantum state resident in GPU memory: a state
+ * vector psi of 2^n complex amplitudes, or a density matrix stored column-major
+ * as the reference stores it (element S[r, c] at r + c*2^n).  Basis index bit
+ * (n-1-q) belongs to qubit q, so qubit 0 is the most significant bit.
+ *
+ * Each entry point names the reference function it replaces (file:line inside
+ * the BraketSimulator.jl project).  All calls return a status code (BS_OK == 0);
+ * on failure bs_last_error() describes the cause.  Host buffers are borrowed for
+ * the duration of a call; nothing is kept.  A handle is not re-entrant, distinct
+ * handles may be used from distinct host threads (each handle owns its stream).
+ */
+#ifndef BRAKET_GB300_H
+#define BRAKET_GB300_H
+#include <stdint.h>
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define BS_OK                0
+#define BS_ERR_INVALID_ARG   1
+#define BS_ERR_CUDA          2
+#define BS_ERR_ALLOC         3
+#define BS_ERR_STATE         4
+#define BS_ERR_UNSUPPORTED   5
+#define BS_ERR_TIMEOUT       6
+
+/* handle kinds and state precision */
+#define BS_KIND_SV           0   /* StateVectorSimulator   (src/sv_simulator.jl:6-42) */
+#define BS_KIND_DM           1   /* DensityMatrixSimulator (src/dm_simulator.jl:6-40) */
+#define BS_PREC_C128         0   /* complex128 state, float-float arithmetic (~2^-46 per op) */
+#define BS_PREC_C64          1   /* complex64 state, FP32 arithmetic, FP64-accurate reductions */
+
+/* gate flags */
+#define BS_GATE_DIAGONAL        0x01u /* matrix holds the 2^k diagonal entries only */
+#define BS_GATE_CONJ            0x02u /* apply conj(U) instead of U (reference Val{true} path) */
+#define BS_GATE_SORTED_TARGETS  0x04u /* matrix bit j <-> j-th largest target qubit (reference >=3-target kernels) */
+#define BS_GATE_MSB_FIRST       0x08u /* matrix bit (k-1-j) <-> targets[j] (big-endian) */
+/* default (no convention flag): matrix index bit j <-> targets[j] */
+
+/* noise modes */
+#define BS_NOISE_REFERENCE      0x00u /* reproduce the reference's block-diagonal Kraus update */
+#define BS_NOISE_PHYSICAL       0x10u /* full channel S <- sum conj(K) S K^T on every element */
+
+/* sampling flags */
+#define BS_ALIAS_EXACT          0x0u  /* bit-exact restatement of the reference's serial table */
+#define BS_ALIAS_PARALLEL       0x1u  /* parallel construction: same distribution, different table */
+
+#define BS_MAX_TARGETS   10
+#define BS_MAX_CONTROLS  16
+
+typedef struct bs_sim bs_sim;
+
+/* One instruction of an operation list.
+ *  kind 0 = gate: matrix is 2^k x 2^k row-major (or 2^k diagonal), interleaved (re, im).
+ *  kind 1 = Kraus channel: n_matrices matrices of 2^k x 2^k, back to back.
+ *  kind 2 = no-op (Measure / Barrier / Reset / Delay, src/dm_simulator.jl:154-157). */
+typedef struct bs_op {
+    int32_t kind;
+    uint32_t flags;
+    int32_t n_targets;
+    int32_t n_controls;
+    int32_t targets[BS_MAX_TARGETS];
+    int32_t controls[BS_MAX_CONTROLS];
+    int32_t control_values[BS_MAX_CONTROLS];
+    int32_t n_matrices;
+    int32_t reserved;
+    const double* matrix;
+} bs_op;
+
+/* Per-handle counters for the last evolve call. */
+typedef struct bs_stats {
+    int64_t sweeps;            /* full passes over the state */
+    int64_t kernel_launches;   /* kernels launched */
+    int64_t gates;             /* gates applied */
+    double  bytes_moved;       /* algorithmic HBM bytes of the executed sweeps */
+    double  gpu_ms;            /* device time of the call (CUDA events) */
+} bs_stats;
+
+/* ---- lifecycle: StateVectorSimulator(T, n, shots) / DensityMatrixSimulator(T, n, shots)
+ *      (src/sv_simulator.jl:53-68, src/dm_simulator.jl:50-65), reinit! (src/sv_simulator.jl:96-127,
+ *      src/dm_simulator.jl:96-128).  The state starts as |0...0> (psi[0] = 1 / S[0,0] = 1). */
+int bs_create(int kind, int n_qubits, int precision, bs_sim** out);
+int bs_destroy(bs_sim* sim);
+int bs_reinit(bs_sim* sim, int n_qubits);
+int bs_qubit_count(const bs_sim* sim, int* out);
+const char* bs_last_error(const bs_sim* sim);
+const char* bs_version(void);
+
+/* ---- state transfer: state_vector / density_matrix / setters
+ *      (src/sv_simulator.jl:150-152, src/dm_simulator.jl:261).
+ *      n_elems = 2^n (SV) or 4^n (DM) complex elements, interleaved doubles. */
+int bs_set_state(bs_sim* sim, const double* host, int64_t n_elems);
+int bs_get_state(bs_sim* sim, double* host, int64_t n_elems);
+/* device-resident variants (pointer to interleaved complex128 on the handle's GPU) */
+int bs_set_state_device(bs_sim* sim, const void* dev, int64_t n_elems);
+int bs_get_state_device(bs_sim* sim, void* dev, int64_t n_elems);
+int bs_copy_state(bs_sim* dst, const bs_sim* src);       /* copyto! (src/sv_simulator.jl:88-94) */
+
+/* ---- gates: apply_gate!(g, psi, targets...) and the dispatch that picks a kernel
+ *      (src/gate_kernels.jl:489-775, src/custom_gates.jl:364-416).
+ *      SV: psi <- C(U) psi, where C(U) applies U on the targets when every control
+ *      qubit c_i has value control_values[i].
+ *      DM: S <- conj(C(U)) S C(U)^T, the two sweeps of _evolve_op! fused into one
+ *      (src/dm_simulator.jl:130-140). */
+int bs_apply_gate(bs_sim* sim, const double* matrix, int n_targets, const int* targets,
+                  int n_controls, const int* controls, const int* control_values, unsigned flags);
+
+/* DM only: one reference apply_gate! call on vec(S) viewed as a 2n-qubit vector
+ * (targets in 0..2n-1).  Used to mirror apply_gate!(Val{conj}, op, vec(S), t...) exactly. */
+int bs_dm_apply_vec_gate(bs_sim* sim, const double* matrix, int n_targets, const int* targets,
+                         int n_controls, const int* controls, const int* control_values, unsigned flags);
+
+/* ---- noise: apply_noise!(kraus, rho, targets...) (src/noise_kernels.jl:102-196).
+ *      flags: BS_NOISE_REFERENCE or BS_NOISE_PHYSICAL plus a target convention flag. */
+int bs_apply_kraus(bs_sim* sim, const double* kraus, int n_kraus, int n_targets, const int* targets,
+                   unsigned flags);
+
+/* ---- evolve!: apply an instruction list (src/sv_simulator.jl:140-148,
+ *      src/dm_simulator.jl:170-179).  Gates are fused into shared-memory tiles. */
+int bs_evolve(bs_sim* sim, const bs_op* ops, int64_t n_ops, unsigned noise_mode);
+int bs_last_stats(const bs_sim* sim, bs_stats* out);
+
+/* ---- probabilities (src/sv_simulator.jl:271, src/dm_simulator.jl:262) */
+int bs_probabilities(bs_sim* sim, double* host_out, int64_t n);
+/* marginal_probability (src/result_types.jl:96-113): sum over the qubits not in targets,
+ * output index bit (k-1-j) <-> targets[j] after the reference's sort of targets. */
+int bs_marginal_probabilities(bs_sim* sim, int n_targets, const int* targets, double* host_out);
+
+/* ---- expectations (src/sv_simulator.jl:240-248, src/dm_simulator.jl:253-260,
+ *      src/result_types.jl:161-167,196-221).
+ * Pauli strings: term t is coeffs[t] * prod_q P_q with P_q = X where x bit set and z unset,
+ * Z where z set and x unset, Y where both set (bit q <-> qubit q).  out[t] = real expectation
+ * of the whole term (coefficient included); one fused read of the state for all terms. */
+int bs_expectation_pauli(bs_sim* sim, int n_terms, const uint64_t* xmask, const uint64_t* zmask,
+                         const double* coeffs, double* out);
+/* Hermitian matrix observable on k targets (reference convention flags as for gates). */
+int bs_expectation_matrix(bs_sim* sim, const double* matrix, int n_targets, const int* targets,
+                          unsigned flags, double* out);
+
+/* ---- sampling (src/result_types.jl:8-80).
+ * bs_alias_build: build the alias table from the current probabilities.  wsum <= 0 lets the
+ * library compute sum(p); pass the reference's wsum for a bit-exact table.
+ * bs_sample_alias: out[s] = u[s] < ap[j[s]] ? j[s] : alias[j[s]] on a supplied stream.
+ * bs_sample_direct: StatsBase inverse-CDF draw used by the reference at >= 30 qubits.
+ * bs_sample: draws with the library's own counter-based generator (seeded). */
+int bs_alias_build(bs_sim* sim, double wsum, unsigned flags);
+/* same table from a supplied probability vector (the reference's own weights) */
+int bs_alias_build_from(bs_sim* sim, const double* probs, int64_t n, double wsum);
+int bs_alias_table(bs_sim* sim, double* ap_out, int64_t* alias_out, int64_t n);
+int bs_sample_alias(bs_sim* sim, const int64_t* j, const double* u, int64_t shots, int64_t* out);
+int bs_sample_direct(bs_sim* sim, const double* u, int64_t shots, double wsum, int64_t* out);
+int bs_sample(bs_sim* sim, uint64_t seed, int64_t shots, int64_t* out);
+
+/* ---- adjoint differentiation (no reference counterpart: the reference declares
+ * AdjointGradient in src/results.jl:90-159 but rejects it, src/pragmas.jl:67-68).
+ * ops: a parameterised circuit; param_index[i] >= 0 marks op i as exp(-i theta G/2) with
+ * generator given by gen_xmask/gen_zmask (Pauli string, Rx/Ry/Rz/XX/YY/ZZ) or as a
+ * PhaseShift when gen_kind[i] == 1.  H = sum_t coeffs[t] P_t.  Writes <H> and dE/dtheta_p. */
+int bs_adjoint_gradient(bs_sim* sim, const bs_op* ops, int64_t n_ops, const int32_t* param_index,
+                        const int32_t* gen_kind, const uint64_t* gen_xmask, const uint64_t* gen_zmask,
+                        int n_params, int n_terms, const uint64_t* xmask, const uint64_t* zmask,
+                        const double* coeffs, double* energy_out, double* grad_out);
+
+/* synchronise the handle's stream; device pointer of the state (for in-HBM benchmarking) */
+int bs_synchronize(bs_sim* sim);
+int bs_state_device_ptr(bs_sim* sim, void** out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

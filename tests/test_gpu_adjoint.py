@@ -1,0 +1,63 @@
+"""Adjoint gradients vs the parameter-shift rule (exact for these generators) and
+central finite differences."""
+import numpy as np
+import pytest
+
+from conftest import bs
+
+pytestmark = pytest.mark.gpu
+from importlib import import_module  # noqa: E402
+
+adj = import_module("braketsimulator_gb300.adjoint")
+
+
+def ansatz(n, layers, rng):
+    ops = []
+    for _ in range(layers):
+        for q in range(n):
+            ops.append(bs.Instruction(bs.Ry(float(rng.uniform(-np.pi, np.pi))), [q]))
+            ops.append(bs.Instruction(bs.Rz(float(rng.uniform(-np.pi, np.pi))), [q]))
+        for q in range(n):
+            ops.append(bs.Instruction(bs.ZZ(float(rng.uniform(-np.pi, np.pi))), [q, (q + 1) % n]))
+    return ops
+
+
+def hamiltonian(n, terms, rng):
+    h = []
+    for _ in range(terms):
+        w = int(rng.integers(1, min(4, n) + 1))
+        qs = rng.choice(n, w, replace=False)
+        h.append((float(rng.normal()), {int(q): "XYZ"[rng.integers(3)] for q in qs}))
+    return h
+
+
+@pytest.mark.parametrize("n,layers", [(2, 1), (4, 2), (7, 2), (12, 2)])
+def test_adjoint_matches_parameter_shift(n, layers):
+    rng = np.random.default_rng(n)
+    ops = ansatz(n, layers, rng)
+    h = hamiltonian(n, 8, rng)
+    sim = bs.StateVectorSimulator(n, 0)
+    e, g = adj.adjoint_gradient(sim, ops, h)
+    e_ref = adj.energy(sim, ops, h)
+    ps = adj.parameter_shift_gradient(sim, ops, h)
+    assert abs(e - e_ref) < 1e-12
+    assert np.max(np.abs(g - ps)) < 1e-10
+
+
+def test_adjoint_other_generators_and_shared_parameters():
+    rng = np.random.default_rng(4)
+    n = 5
+    ops = [bs.Instruction(bs.H(), [q]) for q in range(n)]
+    ops += [bs.Instruction(bs.Rx(0.3), [0]), bs.Instruction(bs.XX(0.7), [1, 3]), bs.Instruction(bs.YY(-0.4), [2, 4]),
+            bs.Instruction(bs.PhaseShift(1.1), [2]), bs.Instruction(bs.CNot(), [0, 4]), bs.Instruction(bs.Rx(0.3), [3])]
+    h = hamiltonian(n, 6, rng)
+    sim = bs.StateVectorSimulator(n, 0)
+    e, g = adj.adjoint_gradient(sim, ops, h)
+    ps = adj.parameter_shift_gradient(sim, ops, h)
+    fd = adj.finite_difference_gradient(sim, ops, h)
+    assert np.max(np.abs(g - ps)) < 1e-10
+    assert np.max(np.abs(g - fd)) < 1e-6
+    # shared parameter: both Rx gates use slot 0
+    pidx = [-1] * n + [0, 1, 2, 3, -1, 0]
+    e2, g2 = adj.adjoint_gradient(sim, ops, h, pidx)
+    assert abs(g2[0] - (g[0] + g[5])) < 1e-12

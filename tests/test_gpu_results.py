@@ -1,0 +1,187 @@
+"""Probabilities, expectations, variances, marginals and sampling on the GPU."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import bs, random_circuit, rel_err
+from golden import reference_kats as K
+
+pytestmark = pytest.mark.gpu
+O = bs.observables
+
+
+def _state_sim(kind):
+    if kind == "sv":
+        s = bs.StateVectorSimulator(4, 1000)
+        s.state_vector = K.RT_STATE
+    else:
+        s = bs.DensityMatrixSimulator(4, 1000)
+        s.density_matrix = np.outer(K.RT_STATE, K.RT_STATE.conj()).T   # stored matrix is rho^T
+    return s
+
+
+def _diag_expect(vec_or_rho, targets, evs, kind):
+    p = np.abs(vec_or_rho) ** 2 if kind == "sv" else np.real(np.diag(vec_or_rho))
+    m = bs.marginal_probability(p, 4, targets)
+    return float(np.dot(m, evs))
+
+
+OBS = [
+    (O.TensorProduct([O.X(), O.H()]), (1, 2)),
+    (O.TensorProduct([O.I(), O.Y()]), (0, 2)),
+    (O.Y(), (2,)),
+]
+
+
+@pytest.mark.parametrize("kind", ["sv", "dm"])
+@pytest.mark.parametrize("obs", OBS, ids=repr)
+def test_expectation_and_variance_vs_diagonalisation(kind, obs):
+    # test/test_result_types.jl:140-180
+    sim = _state_sim(kind)
+    sim.apply_observables([obs])
+    rotated = sim.state_with_observables()
+    evs = obs[0].eigvals()
+    e = bs.calculate(bs.Expectation(*obs), sim)
+    assert abs(e - _diag_expect(rotated, list(obs[1]), evs, kind)) < 1e-12
+    v = bs.calculate(bs.Variance(*obs), sim)
+    p = np.abs(rotated) ** 2 if kind == "sv" else np.real(np.diag(rotated))
+    m = bs.marginal_probability(p, 4, list(obs[1]))
+    assert abs(v - (np.dot(m, evs ** 2) - np.dot(m, evs) ** 2)) < 1e-12
+
+
+@pytest.mark.parametrize("kind", ["sv", "dm"])
+@pytest.mark.parametrize("obs", [O.X(), O.Y(), O.Z(), O.H(), O.I(), O.HermitianObservable([[0.0, 1.0], [1.0, 0.0]])], ids=repr)
+def test_all_qubit_expectations(kind, obs):
+    sim = _state_sim(kind)
+    vals = bs.calculate(bs.Expectation(obs, (0, 1, 2, 3)), sim)
+    for t, val in zip(range(4), vals):
+        s2 = _state_sim(kind)
+        s2.apply_observables([(obs, [t])])
+        r = s2.state_with_observables()
+        assert abs(val - _diag_expect(r, [t], obs.eigvals(), kind)) < 1e-12
+
+
+@pytest.mark.parametrize("kind", ["sv", "dm"])
+def test_probability_and_density_matrix_results(kind):
+    sim = _state_sim(kind)
+    p = np.abs(K.RT_STATE) ** 2
+    assert rel_err(bs.calculate(bs.Probability((0, 1, 2, 3)), sim), p) < 1e-14
+    m12 = [p[[0, 1, 8, 9]].sum(), p[[2, 3, 10, 11]].sum(), p[[4, 5, 12, 13]].sum(), p[[6, 7, 14, 15]].sum()]
+    assert rel_err(bs.calculate(bs.Probability((1, 2)), sim), m12) < 1e-13
+    assert rel_err(bs.calculate(bs.Probability((3, 2, 1, 0)), sim), p) < 1e-14
+    if kind == "sv":
+        amp = bs.calculate(bs.Amplitude(["0010", "0101", "1110"]), sim)
+        assert abs(amp["0010"] - K.RT_STATE[2]) < 1e-15 and abs(amp["1110"] - K.RT_STATE[14]) < 1e-15
+        assert np.allclose(bs.calculate(bs.DensityMatrix((3,)), sim), K.RT_DM_3, rtol=1e-6)
+        assert np.allclose(bs.calculate(bs.DensityMatrix((0, 2, 1)), sim), K.RT_DM_021, rtol=1e-6, atol=1e-7)
+
+
+@pytest.mark.parametrize("n", [3, 9, 14])
+def test_pauli_expectations_random(n):
+    rng = np.random.default_rng(n)
+    ops = random_circuit(n, 40, rng)
+    sim = bs.StateVectorSimulator(n, 0).evolve(ops)
+    psi = oracle.OracleSV(n).evolve(ops).psi
+    for _ in range(12):
+        x = int(rng.integers(0, 2 ** n))
+        z = int(rng.integers(0, 2 ** n))
+        xm = np.array([x], dtype=np.uint64)
+        zm = np.array([z], dtype=np.uint64)
+        out = np.empty(1)
+        sim._h.call("bs_expectation_pauli", 1, bs._abi.u64ptr(xm), bs._abi.u64ptr(zm), bs._abi.dptr(np.ones(1)), bs._abi.dptr(out))
+        assert abs(out[0] - oracle.expectation_pauli_sv(psi, n, x, z)) < 1e-12
+
+
+@pytest.mark.parametrize("n", [2, 5])
+def test_pauli_expectations_dm(n):
+    rng = np.random.default_rng(n + 10)
+    ops = random_circuit(n, 25, rng) + [bs.Instruction(bs.Depolarizing(0.1), [0])]
+    sim = bs.DensityMatrixSimulator(n, 0).evolve(ops)
+    rho = oracle.OracleDM(n).evolve(ops).rho
+    for _ in range(10):
+        x, z = int(rng.integers(0, 2 ** n)), int(rng.integers(0, 2 ** n))
+        out = np.empty(1)
+        sim._h.call("bs_expectation_pauli", 1, bs._abi.u64ptr(np.array([x], dtype=np.uint64)),
+                    bs._abi.u64ptr(np.array([z], dtype=np.uint64)), bs._abi.dptr(np.ones(1)), bs._abi.dptr(out))
+        assert abs(out[0] - oracle.expectation_pauli_dm(rho, n, x, z)) < 1e-12
+
+
+def test_hermitian_multi_target_expectation():
+    rng = np.random.default_rng(11)
+    n = 6
+    ops = random_circuit(n, 30, rng)
+    a = rng.normal(size=(8, 8)) + 1j * rng.normal(size=(8, 8))
+    h = a + a.conj().T
+    for kind in ("sv", "dm"):
+        sim = (bs.StateVectorSimulator if kind == "sv" else bs.DensityMatrixSimulator)(n, 0).evolve(ops)
+        for t in ([4, 1, 2], [0, 5, 3]):
+            e = sim.expectation(O.HermitianObservable(h), *t)
+            # oracle: rotate into the eigenbasis and weight the marginal by eigenvalues
+            w, v = np.linalg.eigh(h)
+            if kind == "sv":
+                psi = oracle.OracleSV(n).evolve(ops).psi
+                phi = psi.copy()
+                oracle.apply_gate(bs.Unitary(v.conj().T), phi, t)
+                m = bs.marginal_probability(np.abs(phi) ** 2, n, t)
+            else:
+                r = oracle.OracleDM(n).evolve(ops)
+                rr = r.rho.copy()
+                oracle.apply_gate(bs.Unitary(v.conj().T), rr, t)
+                oracle.apply_gate(bs.Unitary(v.conj().T), rr, [n + q for q in t], conj=True)
+                d = 2 ** n
+                m = bs.marginal_probability(np.real(rr[:: d + 1]), n, t)
+            # eigenvalue order follows the sorted-target convention of both kernels
+            assert abs(e - float(np.dot(m, w))) < 1e-10, (kind, t)
+
+
+# ---------------------------------------------------------------- sampling
+@pytest.mark.parametrize("n", [1, 4, 10, 16])
+def test_alias_bit_exact_on_supplied_stream(n):
+    rng = np.random.default_rng(n)
+    p = rng.random(2 ** n) ** 4
+    p /= p.sum()
+    ws = oracle.pairwise_sum(p)
+    shots = 5000
+    j = rng.integers(0, 2 ** n, shots)
+    u = rng.random(shots)
+    sim = bs.StateVectorSimulator(n, shots)
+    got = sim.samples_from_stream(j, u, wsum=ws, probabilities=p)
+    ap, al = oracle.alias_table(p, ws)
+    gap, gal = sim.alias_table()
+    assert np.array_equal(gap, ap) and np.array_equal(gal, al)
+    assert np.array_equal(got, oracle.sample_alias(ap, al, j, u))
+
+
+@pytest.mark.parametrize("n", [6, 12, 18])
+def test_direct_sampling_matches_linear_scan(n):
+    rng = np.random.default_rng(n + 1)
+    ops = random_circuit(n, 30, rng)
+    sim = bs.StateVectorSimulator(n, 0).evolve(ops)
+    p = sim.probabilities()
+    u = rng.random(20000)
+    got = sim.samples_direct(u, wsum=float(np.sum(p)))
+    ref = oracle.sample_direct(p, u, float(np.sum(p)))
+    mismatches = int(np.sum(got != ref))
+    assert mismatches <= 2, mismatches      # only possible at FP boundaries of the running sum
+
+
+def test_sample_statistics():
+    # test/test_sv_simulator.jl:385-398 (Bell pair, 10000 shots)
+    sim = bs.StateVectorSimulator(2, 10000).evolve([bs.Instruction(bs.H(), [0]), bs.Instruction(bs.CNot(), [0, 1])])
+    s = sim.samples(seed=99)
+    vals, counts = np.unique(s, return_counts=True)
+    assert list(vals) == [0, 3] and counts.sum() == 10000 and 0.4 < counts[0] / 10000 < 0.6
+    dm = bs.DensityMatrixSimulator(2, 10000).evolve([bs.Instruction(bs.H(), [0]), bs.Instruction(bs.CNot(), [0, 1])])
+    s = dm.samples(seed=7)
+    vals, counts = np.unique(s, return_counts=True)
+    assert list(vals) == [0, 3] and 0.4 < counts[0] / 10000 < 0.6
+
+
+def test_simulate_program_ghz_batch():
+    # test/test_sv_simulator.jl:399-419
+    prog = bs.Program([bs.Instruction(bs.H(), [0])] + [bs.Instruction(bs.CNot(), [0, k]) for k in range(1, 5)])
+    res = bs.simulate(bs.StateVectorSimulator(5, 0), [prog] * 4, 1000, seed=5)
+    for r in res:
+        m = r["measurements"]
+        assert m.shape == (1000, 5)
+        assert 400 < np.sum(np.all(m == 0, axis=1)) < 600 and 400 < np.sum(np.all(m == 1, axis=1)) < 600

@@ -1,0 +1,153 @@
+"""State-vector parity: GB300 engine vs the reference's golden vectors and vs the
+CPU oracle.  Amplitudes must agree within 1e-12 relative (norm-wise, Julia's
+isapprox definition) with the FP64 oracle."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import bs, make_op, random_circuit, rel_err
+from golden import reference_kats as K
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+@pytest.mark.parametrize("case", K.SV_KATS + K.CUSTOM_KATS, ids=lambda c: "+".join(s[0] for s in c[0]))
+def test_sv_kats(case):
+    ins, n, sv, probs = case
+    ops = [make_op(s) for s in ins]
+    sim = bs.StateVectorSimulator(n, 0).evolve(ops)
+    got = sim.state_vector
+    ref = oracle.OracleSV(n).evolve(ops).psi
+    assert rel_err(got, ref) < TOL
+    assert rel_err(got, sv) < 1e-7
+    if probs is not None:
+        assert rel_err(sim.probabilities(), probs) < 1e-7
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 8, 11, 13, 16])
+@pytest.mark.parametrize("pows", [False, True])
+def test_random_circuits(n, pows):
+    rng = np.random.default_rng(1000 * n + pows)
+    ops = random_circuit(n, 60 if n < 13 else 40, rng, pows=pows)
+    sim = bs.StateVectorSimulator(n, 0).evolve(ops)
+    ref = oracle.OracleSV(n).evolve(ops).psi
+    assert rel_err(sim.state_vector, ref) < TOL
+
+
+@pytest.mark.parametrize("n", [14, 18, 20])
+def test_deep_layers(n):
+    """Dense SU(2) layers with CZ bricks (the 30-qubit benchmark's structure) at oracle size."""
+    rng = np.random.default_rng(n)
+    ops = []
+    for layer in range(12):
+        for q in range(n):
+            a = rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2))
+            u, _ = np.linalg.qr(a)
+            ops.append(bs.Instruction(bs.Unitary(u), [q]))
+        for q in range(layer % 2, n - 1, 2):
+            ops.append(bs.Instruction(bs.CZ(), [q, q + 1]))
+    sim = bs.StateVectorSimulator(n, 0).evolve(ops)
+    ref = oracle.OracleSV(n).evolve(ops).psi
+    assert rel_err(sim.state_vector, ref) < TOL
+    st = sim.last_stats()
+    assert st["sweeps"] < len(ops)   # gates were fused into tiles
+
+
+def test_ghz10():
+    ops = [bs.Instruction(bs.H(), [0])] + [bs.Instruction(bs.CNot(), [0, k]) for k in range(1, 10)]
+    sim = bs.StateVectorSimulator(10, 1000).evolve(ops)
+    p = sim.probabilities()
+    exp = np.zeros(1024)
+    exp[0] = exp[-1] = 0.5
+    assert np.allclose(p, exp, atol=1e-15)
+    s = sim.samples(seed=3)
+    assert s.shape == (1000,) and set(np.unique(s)) <= {0, 1023}
+    assert 400 < np.sum(s == 0) < 600
+
+
+@pytest.mark.parametrize("n", [4, 8, 12, 16, 20])
+def test_qft_uniform(n):
+    # test/test_sv_simulator.jl:360-384
+    ops = []
+    for t in range(n):
+        ops.append(bs.Instruction(bs.H(), [t]))
+        ang = math.pi / 2
+        for c in range(t + 1, n):
+            ops.append(bs.Instruction(bs.CPhaseShift(ang), [c, t]))
+            ang /= 2
+    sim = bs.StateVectorSimulator(n, 0).evolve(ops)
+    assert rel_err(sim.probabilities(), np.full(2 ** n, 1 / 2 ** n)) < 1e-12
+
+
+@pytest.mark.parametrize("nq", [1, 2, 3, 4])
+def test_gphase_and_control_gphase(nq):
+    phi = 2.12
+    hs = [bs.Instruction(bs.H(), [q]) for q in range(nq)]
+    for g in (bs.GPhase(nq, phi), bs.Control(bs.GPhase(nq, phi), (0,) * nq), bs.MultiRZ(phi)):
+        ops = hs + [bs.Instruction(g, list(range(nq)))]
+        sim = bs.StateVectorSimulator(nq, 0).evolve(ops)
+        assert rel_err(sim.state_vector, oracle.OracleSV(nq).evolve(ops).psi) < TOL
+
+
+def test_controls_negctrl_and_unitary_big():
+    rng = np.random.default_rng(5)
+    n = 9
+    ops = [bs.Instruction(bs.H(), [q]) for q in range(n)]
+    ops.append(bs.Instruction(bs.Control(bs.U(0.3, 0.2, 0.1), (0,)), [7, 2]))
+    ops.append(bs.Instruction(bs.Control(bs.Ry(0.7), (1, 0)), [0, 8, 4]))
+    ops.append(bs.Instruction(bs.Control(bs.Swap(), (1,)), [3, 1, 6]))
+    q, _ = np.linalg.qr(rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32)))
+    ops.append(bs.Instruction(bs.Unitary(q), [6, 0, 3, 8, 2]))       # 5 targets: sorted convention
+    sim = bs.StateVectorSimulator(n, 0).evolve(ops)
+    assert rel_err(sim.state_vector, oracle.OracleSV(n).evolve(ops).psi) < TOL
+
+
+def test_inverse_roundtrip():
+    # test/test_gate_operations.jl: g then inv(g) is the identity on a superposition
+    from conftest import GATES_1, GATES_A
+    nq = 4
+    hs = [bs.Instruction(bs.H(), [q]) for q in range(nq)]
+    base = bs.StateVectorSimulator(nq, 0).evolve(hs).state_vector
+    gates = [GATES_1[n]() for n in ["x", "y", "z", "h", "s", "si", "t", "ti", "v", "vi", "cnot", "cy", "cz", "cv", "swap", "iswap", "ecr"]]
+    gates += [GATES_A[n](0.23) for n in ["rx", "ry", "rz", "phaseshift", "gpi", "gpi2", "xx", "yy", "zz", "xy", "pswap", "cphaseshift", "single_excitation"]]
+    for g in gates:
+        t = list(range(g.qubit_count()))
+        sim = bs.StateVectorSimulator(nq, 0).evolve(hs + [bs.Instruction(g, t), bs.Instruction(g.inv(), t)])
+        assert rel_err(sim.state_vector, base) < 1e-12, g
+
+
+def test_errors_are_reported_not_faulted():
+    sim = bs.StateVectorSimulator(3, 0)
+    with pytest.raises(bs._abi.BraketGB300Error):
+        sim.evolve([bs.Instruction(bs.H(), [5])])
+    with pytest.raises(bs._abi.BraketGB300Error):
+        sim.evolve([bs.Instruction(bs.CNot(), [1, 1])])
+    # handle still usable
+    sim.evolve([bs.Instruction(bs.X(), [0])])
+    assert abs(sim.state_vector[4] - 1) < 1e-15
+
+
+def test_zero_and_one_qubit():
+    sim = bs.StateVectorSimulator(0, 10)
+    assert np.allclose(sim.state_vector, [1.0])
+    assert np.allclose(sim.probabilities(), [1.0])
+    assert list(sim.samples(seed=1)) == [0] * 10
+    sim.reinit(1, 0)
+    sim.evolve([bs.Instruction(bs.Rx(0.15), [0])])
+    assert rel_err(sim.state_vector, [0.99718882, -0.07492971j]) < 1e-7
+
+
+def test_reinit_copy_copyto():
+    # test/test_sv_simulator.jl: similar, copy and copyto!
+    sim = bs.StateVectorSimulator(10, 0)
+    v = np.exp(1j * np.arange(1024)) / 32
+    sim.state_vector = v
+    c = sim.copy()
+    assert rel_err(c.state_vector, v) == 0
+    d = bs.StateVectorSimulator(10, 0).copyto(sim)
+    assert rel_err(d.state_vector, v) == 0
+    sim.reinit(10, 5)
+    assert sim.state_vector[0] == 1 and np.count_nonzero(sim.state_vector) == 1
