@@ -1,0 +1,326 @@
+"""Benchmark: 30-qubit complex128 state-vector gate layers on one GB300.
+
+Workload (one "step"): the dense random circuit on 30 qubits — 20 layers of a
+Haar-random SU(2) on every qubit followed by CZ on an alternating even/odd
+brick, then 20 layers of SU(2) on every qubit followed by CZ at (q, q+s mod 30)
+with s cycling through 1, 8, 16 — then <Z0 Z29> and 1e5 shots, run from |0...0>
+through the public API.  Data are seeded synthetic circuits (no dataset exists).
+
+value   : executed-sweep HBM bytes of the gate layers (2*16*2^30 B per sweep)
+          / device time of the evolution (CUDA events on the launching stream).
+e2e     : the same bytes / wall time of the whole step through the public API
+          (circuit upload, evolution, expectation, shots copied to the host).
+Side measurement: adjoint gradients of the 24-qubit, 720-parameter ansatz with a
+48-term Hamiltonian, against parameter shift on the same GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_QUBITS = 30
+LAYERS = 20
+SHOTS = 100_000
+STRIDES = (1, 8, 16)
+
+
+def load():
+    import __graft_entry__ as ge
+    ge.build()
+    return ge.load_package()
+
+
+def haar_su2(rng):
+    a = rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2))
+    q, r = np.linalg.qr(a)
+    q = q * (np.diag(r) / np.abs(np.diag(r)))
+    return q / np.sqrt(np.linalg.det(q))
+
+
+def dense_circuit(bs, n=N_QUBITS, layers=LAYERS, seed=0):
+    rng = np.random.default_rng(seed)
+    ops = []
+    for layer in range(layers):
+        for q in range(n):
+            ops.append(bs.Instruction(bs.Unitary(haar_su2(rng)), [q]))
+        for q in range(layer % 2, n - 1, 2):
+            ops.append(bs.Instruction(bs.CZ(), [q, q + 1]))
+    for layer in range(layers):
+        s = STRIDES[layer % len(STRIDES)]
+        for q in range(n):
+            ops.append(bs.Instruction(bs.Unitary(haar_su2(rng)), [q]))
+        used = set()
+        for q in range(n):
+            r = (q + s) % n
+            if q in used or r in used:
+                continue
+            used.update((q, r))
+            ops.append(bs.Instruction(bs.CZ(), [q, r]))
+    return ops
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and r[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def step(bs, sim, ops, shots, seed):
+    """One simulate-style pass through the public API; returns (evolve device ms, stats, result)."""
+    sim.reinit(N_QUBITS, shots)
+    sim.evolve(ops)
+    st = sim.last_stats()
+    zz = bs.observables.TensorProduct([bs.observables.Z(), bs.observables.Z()])
+    e = sim.expectation(zz, 0, N_QUBITS - 1)
+    s = sim.samples(seed)
+    return st, e, s
+
+
+def cpu_baseline_port(seconds_budget=20.0):
+    """The oracle (C restatement of the reference's kernels, OpenMP over host cores) on a
+    bounded sample of the workload: SU(2) sweeps and CZ sweeps of the 30-qubit state."""
+    import oracle
+    L = oracle.lib()
+    n = N_QUBITS
+    psi = np.zeros(2 ** n, dtype=np.complex128)
+    psi[0] = 1.0
+    rng = np.random.default_rng(1)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    sweeps = 0
+    q = 0
+    while time.perf_counter() - t0 < seconds_budget and sweeps < 64:
+        u = np.ascontiguousarray(haar_su2(rng))
+        L.orc_apply_1q(psi.ctypes.data, psi.size, u.ctypes.data, q)
+        sweeps += 1
+        if sweeps % 3 == 0:
+            cz = np.ascontiguousarray(np.diag([1, 1, 1, -1]).astype(np.complex128))
+            L.orc_apply_2q(psi.ctypes.data, psi.size, cz.ctypes.data, q, (q + 1) % n)
+            sweeps += 1
+        q = (q + 7) % n
+    dt = time.perf_counter() - t0
+    gbs = sweeps * 32.0 * 2 ** n / dt / 1e9
+    return {"value": round(gbs, 2), "unit": "GB/s", "cores": cores, "kind": "port",
+            "sample": f"{sweeps} reference-kernel gate sweeps (SU(2) and CZ) of the 30-qubit complex128 state, "
+                      f"{dt:.1f} s on {cores} OpenMP threads"}, dt
+
+
+def adjoint_bench(bs, n=24, layers=10, terms=48, shift_params=24, seed=3):
+    from importlib import import_module
+    adj = import_module("braketsimulator_gb300.adjoint")
+    rng = np.random.default_rng(seed)
+    ops = []
+    for _ in range(layers):
+        for q in range(n):
+            ops.append(bs.Instruction(bs.Ry(float(rng.uniform(-np.pi, np.pi))), [q]))
+            ops.append(bs.Instruction(bs.Rz(float(rng.uniform(-np.pi, np.pi))), [q]))
+        for q in range(n):
+            ops.append(bs.Instruction(bs.ZZ(float(rng.uniform(-np.pi, np.pi))), [q, (q + 1) % n]))
+    h = []
+    for _ in range(terms):
+        w = int(rng.integers(1, 5))
+        qs = rng.choice(n, w, replace=False)
+        h.append((float(rng.normal()), {int(q): "XYZ"[rng.integers(3)] for q in qs}))
+    sim = bs.StateVectorSimulator(n, 0)
+    adj.adjoint_gradient(sim, ops, h)            # warm-up
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        e, g = adj.adjoint_gradient(sim, ops, h)
+    torch.cuda.synchronize()
+    t_adj = (time.perf_counter() - t0) / reps
+    # parameter shift on a subset of parameters (cost is linear in the count)
+    pidx = adj.parameterised(ops)
+    pick = sorted(rng.choice(len(pidx), shift_params, replace=False))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    diffs = []
+    for k in pick:
+        i = pidx[k]
+        ix = ops[i]
+        plus = ops[:i] + [adj._with_angle(ix, math.pi / 2)] + ops[i + 1:]
+        minus = ops[:i] + [adj._with_angle(ix, -math.pi / 2)] + ops[i + 1:]
+        d = (adj.energy(sim, plus, h) - adj.energy(sim, minus, h)) / 2.0
+        diffs.append(abs(d - g[k]))
+    torch.cuda.synchronize()
+    t_ps_per_param = (time.perf_counter() - t0) / shift_params
+    P = len(pidx)
+    return {"qubits": n, "params": P, "terms": terms, "energy": e,
+            "adjoint_s_per_gradient": round(t_adj, 4), "adjoint_grads_per_s": round(P / t_adj, 1),
+            "param_shift_s_per_gradient_extrapolated": round(t_ps_per_param * P, 3),
+            "param_shift_grads_per_s": round(1.0 / t_ps_per_param, 2),
+            "speedup_vs_param_shift": round(t_ps_per_param * P / t_adj, 1),
+            "max_abs_diff_vs_param_shift": float(max(diffs)),
+            "param_shift_sample": f"{shift_params} of {P} parameters, 2 circuits each"}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU kernels (oracle port; Julia is not installed)
+    on the host cores, bounded sample of the same workload per step."""
+    if rank != 0:
+        return
+    import oracle
+    oracle.lib()
+    vals = []
+    for i in range(args.warmup + args.steps):
+        res, dt = cpu_baseline_port(seconds_budget=8.0)
+        if i >= args.warmup:
+            vals.append((res, dt))
+    v = float(np.mean([r["value"] for r, _ in vals]))
+    line = {"impl": "reference", "metric": "30q SV gate-layer HBM GB/s", "value": round(v, 2), "unit": "GB/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1000 * float(np.mean([dt for _, dt in vals])), 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64)", "data": "synthetic",
+            "config": {"workload": "dense random circuit, 30 qubits, complex128 (bounded sample of its gate sweeps)"},
+            "cpu_baseline": {**vals[-1][0], "value": round(v, 2)},
+            "e2e": {"value": round(v, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--qubits", type=int, default=N_QUBITS, help="smaller cases for profiling")
+    args = ap.parse_args()
+    globals()["N_QUBITS"] = args.qubits
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    bs = load()
+    ops = dense_circuit(bs, n=N_QUBITS)
+    sim = bs.StateVectorSimulator(N_QUBITS, SHOTS)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for i in range(args.warmup):
+        step(bs, sim, ops, SHOTS, 100 + i)
+    barrier()
+    dev_ms, bytes_moved, sweeps, launches = 0.0, 0.0, 0, 0
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            st, e, s = step(bs, sim, ops, SHOTS, 1000 + i)
+            dev_ms += st["gpu_ms"]
+            bytes_moved += st["bytes_moved"]
+            sweeps += st["sweeps"]
+            launches += st["kernel_launches"]
+        barrier()
+        wall = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([wall, dev_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        wall, dev_ms = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+    hbm, src = peaks()
+    per_launch_ms = dev_ms / max(1, sweeps)
+    achieved = 32.0 * 2 ** N_QUBITS / (per_launch_ms * 1e-3) / 1e9
+    value = bytes_moved / (dev_ms * 1e-3) / 1e9 * world
+    e2e = bytes_moved / wall / 1e9 * world
+    n_gates = sum(1 for _ in ops)
+    gate_eq = n_gates * 32.0 * 2 ** N_QUBITS * args.steps / (dev_ms * 1e-3) / 1e9
+    line = {
+        "metric": "30q SV gate-layer HBM GB/s", "value": round(value, 1), "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * wall / args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128 state, float-float (FP32-pipe) arithmetic", "data": "synthetic (seeded Haar SU(2) + CZ)",
+        "config": {"workload": "dense random circuit, 30 qubits, complex128, 2x20 layers, <Z0 Z29> + 1e5 shots",
+                   "qubits": N_QUBITS, "gates": n_gates, "shots": SHOTS,
+                   "l2": "state (16 GiB) larger than L2 (129 MB)", "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "e2e": {"value": round(e2e, 1), "unit": "GB/s", "h2d_bytes_per_step": int(n_gates * 64 + 200 * n_gates),
+                "d2h_bytes_per_step": int(SHOTS * 8 + 8)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 3), "traffic": None, "peak_source": src,
+                     "kernel": "k_tile_sweep", "bytes_per_launch": 32 * 2 ** N_QUBITS},
+        "gate_layer": {"sweeps_per_step": sweeps // args.steps, "gates_per_step": n_gates,
+                       "gate_equivalent_GBps": round(gate_eq, 1),
+                       "layer_ms": round(dev_ms / args.steps / (2 * LAYERS), 2)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"], _ = cpu_baseline_port()
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_bench(bs)
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -33,7 +33,7 @@ def build(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     src = os.path.join(HERE, "ref_kernels.c")
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
-        subprocess.run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-o", LIB + ".tmp", src, "-lm"], check=True)
+        subprocess.run(["gcc", "-O2", "-std=c11", "-fopenmp", "-fPIC", "-shared", "-o", LIB + ".tmp", src, "-lm"], check=True)
         os.replace(LIB + ".tmp", LIB)
     return LIB
 

@@ -60,4 +60,4 @@ def test_adjoint_other_generators_and_shared_parameters():
     # shared parameter: both Rx gates use slot 0
     pidx = [-1] * n + [0, 1, 2, 3, -1, 0]
     e2, g2 = adj.adjoint_gradient(sim, ops, h, pidx)
-    assert abs(g2[0] - (g[0] + g[5])) < 1e-12
+    assert abs(g2[0] - (g[0] + g[4])) < 1e-12
