@@ -214,6 +214,68 @@ def adjoint_bench(bs, n=24, layers=10, terms=48, shift_params=24, seed=3):
             "param_shift_sample": f"{shift_params} of {P} parameters, 2 circuits each"}
 
 
+def ghz_bench(bs, reps=100):
+    """GHZ-10 (H, CNOT(0,k)), full probabilities and 1000 shots per circuit: latency-bound."""
+    import torch
+    ops = [bs.Instruction(bs.H(), [0])] + [bs.Instruction(bs.CNot(), [0, k]) for k in range(1, 10)]
+    sim = bs.StateVectorSimulator(10, 1000)
+    for r in range(5):
+        sim.reinit(10, 1000)
+        sim.evolve(ops)
+        sim.probabilities()
+        sim.samples(r)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in range(reps):
+        sim.reinit(10, 1000)
+        sim.evolve(ops)
+        p = sim.probabilities()
+        s = sim.samples(r)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    ok = abs(p[0] - 0.5) < 1e-15 and abs(p[-1] - 0.5) < 1e-15 and set(np.unique(s)) <= {0, 1023}
+    return {"us_per_circuit": round(dt * 1e6, 1), "circuits_per_s": round(1 / dt, 1), "checked": bool(ok)}
+
+
+def dm_circuit(bs, n=14, depth=12, seed=5):
+    rng = np.random.default_rng(seed)
+    ops = []
+    for _ in range(depth):
+        for q in range(n):
+            g = [bs.Rx, bs.Ry, bs.Rz][rng.integers(3)](float(rng.uniform(0, 2 * np.pi)))
+            ops += [bs.Instruction(g, [q]), bs.Instruction(bs.Depolarizing(1e-3), [q]),
+                    bs.Instruction(bs.AmplitudeDamping(5e-3), [q])]
+        for q in range(n - 1):
+            ops += [bs.Instruction(bs.CNot(), [q, q + 1]), bs.Instruction(bs.TwoQubitDepolarizing(1e-2), [q, q + 1]),
+                    bs.Instruction(bs.AmplitudeDamping(5e-3), [q]), bs.Instruction(bs.AmplitudeDamping(5e-3), [q + 1])]
+    return ops
+
+
+def dm_bench(bs, n=14):
+    """Noisy density matrix, 14 qubits (4 GiB): diag + <X X X X> on qubits 0..3, both noise modes."""
+    import torch
+    ops = dm_circuit(bs, n)
+    x4 = bs.observables.TensorProduct([bs.observables.X()] * 4)
+    out = {}
+    for mode in ("reference", "physical"):
+        sim = bs.DensityMatrixSimulator(n, 0, noise_mode=mode)
+        sim.evolve(ops)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.reinit(n, 0)
+        sim.evolve(ops)
+        st = sim.last_stats()
+        diag = sim.probabilities()
+        ex = sim.expectation(x4, 0, 1, 2, 3)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[mode] = {"s_per_circuit": round(dt, 3), "evolve_gpu_ms": round(st["gpu_ms"], 1), "sweeps": st["sweeps"],
+                     "sweep_GBps": round(st["bytes_moved"] / (st["gpu_ms"] * 1e-3) / 1e9, 1),
+                     "trace": round(float(np.sum(diag)), 12), "x4": ex}
+    out["instructions"] = len(ops)
+    return out
+
+
 def run_reference(args, rank, world):
     """--impl reference: the reference's CPU kernels (oracle port; Julia is not installed)
     on the host cores, bounded sample of the same workload per step."""
@@ -319,6 +381,8 @@ def main():
         line["cpu_baseline"], _ = cpu_baseline_port()
     if not args.no_adjoint:
         line["adjoint"] = adjoint_bench(bs)
+        line["ghz10"] = ghz_bench(bs)
+        line["dm14"] = dm_bench(bs)
     print(json.dumps(line), flush=True)
 
 

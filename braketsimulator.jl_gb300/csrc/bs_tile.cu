@@ -38,18 +38,42 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
             if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
     const int ngroups = 1 << (T - K);
     const float4* m = mats + g.mat_off;
+    const uint32_t lcm = g.lc_mask, lcv = g.lc_val;
+    int tb[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) tb[q] = g.tbit[q];
+    if (K == 1) {
+        // 2x2: matrix held in registers across the thread's pairs
+        const cff m00 = f4c(__ldg(m)), m01 = f4c(__ldg(m + 1)), m10 = f4c(__ldg(m + 2)), m11 = f4c(__ldg(m + 3));
+        const int b0 = 1 << tb[0];
+#pragma unroll 2
+        for (int gr = threadIdx.x; gr < ngroups; gr += blockDim.x) {
+            const int jb = insert0(gr, pos[0]);
+            if ((jb & (int)lcm) != (int)lcv) continue;
+            const cff a = f4c(sm[jb]), b = f4c(sm[jb | b0]);
+            ffacc ar, ai;
+            cmac_first(ar, ai, m00, a);
+            cmac(ar, ai, m01, b);
+            const cff ya = cdone(ar, ai);
+            cmac_first(ar, ai, m10, a);
+            cmac(ar, ai, m11, b);
+            sm[jb | b0] = c4f(cdone(ar, ai));
+            sm[jb] = c4f(ya);
+        }
+        return;
+    }
     for (int gr = threadIdx.x; gr < ngroups; gr += blockDim.x) {
         int jb = gr;
 #pragma unroll
         for (int q = 0; q < K; q++) jb = insert0(jb, pos[q]);
-        if ((jb & (int)g.lc_mask) != (int)g.lc_val) continue;
+        if ((jb & (int)lcm) != (int)lcv) continue;
         cff x[D];
         int idx[D];
 #pragma unroll
         for (int c = 0; c < D; c++) {
             int j = jb;
 #pragma unroll
-            for (int q = 0; q < K; q++) if ((c >> q) & 1) j |= 1 << g.tbit[q];
+            for (int q = 0; q < K; q++) if ((c >> q) & 1) j |= 1 << tb[q];
             idx[c] = j;
             x[c] = f4c(sm[j]);
         }
@@ -121,6 +145,9 @@ __device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const flo
     }
 }
 
+// KMAX: widest dense/monomial gate of the sweep (2 or 4); narrow sweeps get a
+// kernel with fewer live registers and therefore more resident warps.
+template <int KMAX>
 __global__ void __launch_bounds__(kThreads) k_tile_sweep(double2* __restrict__ psi, SweepDesc d, int64_t tile0) {
     extern __shared__ float4 smem[];
     const int T = d.T, L = d.L, H = T - L;
@@ -149,24 +176,21 @@ __global__ void __launch_bounds__(kThreads) k_tile_sweep(double2* __restrict__ p
     }
     __syncthreads();
     for (int gi = 0; gi < d.n_gates; gi++) {
-        const TileGate g = d.gates[gi];
+        const TileGate& g = d.gates[gi];
         if ((base & (int64_t)g.gc_mask) != (int64_t)g.gc_val) continue;   // uniform in the CTA
-        if (g.kind == 1) {
+        const int kind = g.kind, k = g.k;
+        if (kind == 1) {
             tile_diag(smem, T, L, g, d.mats, base, off_tab);
-        } else if (g.kind == 0) {
-            switch (g.k) {
-                case 1: tile_dense<1>(smem, T, g, d.mats); break;
-                case 2: tile_dense<2>(smem, T, g, d.mats); break;
-                case 3: tile_dense<3>(smem, T, g, d.mats); break;
-                default: tile_dense<4>(smem, T, g, d.mats); break;
-            }
+        } else if (kind == 0) {
+            if (k == 1) tile_dense<1>(smem, T, g, d.mats);
+            else if (k == 2 || KMAX == 2) tile_dense<2>(smem, T, g, d.mats);
+            else if (KMAX > 2 && k == 3) tile_dense<3>(smem, T, g, d.mats);
+            else if (KMAX > 2) tile_dense<4>(smem, T, g, d.mats);
         } else {
-            switch (g.k) {
-                case 1: tile_monomial<1>(smem, T, g, d.perms); break;
-                case 2: tile_monomial<2>(smem, T, g, d.perms); break;
-                case 3: tile_monomial<3>(smem, T, g, d.perms); break;
-                default: tile_monomial<4>(smem, T, g, d.perms); break;
-            }
+            if (k == 1) tile_monomial<1>(smem, T, g, d.perms);
+            else if (k == 2 || KMAX == 2) tile_monomial<2>(smem, T, g, d.perms);
+            else if (KMAX > 2 && k == 3) tile_monomial<3>(smem, T, g, d.perms);
+            else if (KMAX > 2) tile_monomial<4>(smem, T, g, d.perms);
         }
         __syncthreads();
     }
@@ -247,7 +271,7 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     std::vector<TileGate> tg;
     std::vector<float4> mats;
     std::vector<int32_t> perms;
-    struct Launch { int64_t gate0; int n_gates; std::vector<int> hi; bool big; int big_gate; };
+    struct Launch { int64_t gate0; int n_gates; std::vector<int> hi; bool big; int big_gate; int kmax = 1; };
     std::vector<Launch> launches;
     std::vector<int32_t> big_bits;
     for (const Sweep& sw : sweeps) {
@@ -321,6 +345,7 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
             } else {
                 perms.insert(perms.end(), hg.perm.begin(), hg.perm.end());
             }
+            if (hg.kind != 1) ln.kmax = std::max(ln.kmax, hg.k);
             tg.push_back(t);
             ln.n_gates++;
         }
@@ -351,7 +376,11 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     const size_t smem = ((size_t)1 << T) * sizeof(float4) + ((size_t)1 << H) * sizeof(int64_t);
     static bool attr_set[64] = {false};
     if (!attr_set[s->device & 63]) {
-        cudaFuncSetAttribute(k_tile_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        cudaFuncSetAttribute(k_tile_sweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        cudaFuncSetAttribute(k_tile_sweep<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        // largest carveout: three 65 KiB tiles per SM instead of two
+        cudaFuncSetAttribute(k_tile_sweep<2>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+        cudaFuncSetAttribute(k_tile_sweep<4>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         cudaFuncSetAttribute(k_dense_big, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
         attr_set[s->device & 63] = true;
     }
@@ -387,7 +416,8 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         d.perms = d_p;
         for (int64_t t0 = 0; t0 < ntiles; t0 += (1LL << 30)) {
             int64_t nb = std::min<int64_t>(ntiles - t0, 1LL << 30);
-            k_tile_sweep<<<(unsigned)nb, kThreads, smem, s->stream>>>(psi, d, t0);
+            if (ln.kmax <= 2) k_tile_sweep<2><<<(unsigned)nb, kThreads, smem, s->stream>>>(psi, d, t0);
+            else k_tile_sweep<4><<<(unsigned)nb, kThreads, smem, s->stream>>>(psi, d, t0);
         }
         s->stats.kernel_launches++;
         s->stats.sweeps++;
