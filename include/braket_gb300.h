@@ -166,6 +166,23 @@ int bs_adjoint_gradient(bs_sim* sim, const bs_op* ops, int64_t n_ops, const int3
                         int n_params, int n_terms, const uint64_t* xmask, const uint64_t* zmask,
                         const double* coeffs, double* energy_out, double* grad_out);
 
+/* ---- allocation-free Pauli expectations.  No counterpart in the reference: it serves
+ * callers that cannot allocate device memory when they need an expectation value (a runtime
+ * that owns all of HBM through its own pool, a real-time loop that cannot afford the device
+ * synchronisation of cudaMalloc/cudaFree).  Same terms and result as bs_expectation_pauli,
+ * computed from a complex128 state the caller holds at state_dev (kind BS_KIND_SV: 2^n
+ * amplitudes; BS_KIND_DM: the stored matrix, column-major 4^n elements), on `stream`
+ * (a cudaStream_t, NULL for the default stream); `out` is host memory.
+ * Scratch: one static 256 KiB device array inside the library, present on every GPU that
+ * loads it until the process exits; no cudaMalloc/cudaFree or other allocation is made.
+ * Limits: n_terms <= 32 and n_qubits <= 34 (SV) / 17 (DM); larger requests return
+ * BS_ERR_UNSUPPORTED.  The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  Every call reuses the
+ * same array, so calls that can overlap on the GPU race and must be serialised by the caller. */
+int bs_expectation_pauli_noalloc(const void* state_dev, int kind, int n_qubits, int n_terms,
+                                 const uint64_t* xmask, const uint64_t* zmask, const double* coeffs,
+                                 double* out, void* stream);
+
 /* synchronise the handle's stream; device pointer of the state (for in-HBM benchmarking) */
 int bs_synchronize(bs_sim* sim);
 int bs_state_device_ptr(bs_sim* sim, void** out);
