@@ -308,6 +308,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--qubits", type=int, default=N_QUBITS, help="smaller cases for profiling")
+    ap.add_argument("--precision", default="c128", choices=["c128", "c64"])
     args = ap.parse_args()
     globals()["N_QUBITS"] = args.qubits
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -322,7 +323,7 @@ def main():
         dist.init_process_group("nccl")
     bs = load()
     ops = dense_circuit(bs, n=N_QUBITS)
-    sim = bs.StateVectorSimulator(N_QUBITS, SHOTS)
+    sim = bs.StateVectorSimulator(N_QUBITS, SHOTS, precision=args.precision)
 
     def barrier():
         if world > 1:

@@ -311,6 +311,7 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
                                    const double* coeffs, double* energy_out, double* grad_out) {
     if (!s) return BS_ERR_INVALID_ARG;
     if (s->kind != BS_KIND_SV) return bs_fail(s, BS_ERR_UNSUPPORTED, "adjoint gradients need a state-vector simulator");
+    if (s->precision != BS_PREC_C128) return bs_fail(s, BS_ERR_UNSUPPORTED, "adjoint gradients need a complex128 state");
     if (n_ops < 0 || (n_ops && (!ops || !param_index || !gen_kind || !gen_xmask || !gen_zmask)) || n_params < 0 ||
         n_terms < 1 || !xmask || !zmask || !coeffs || !energy_out || (n_params && !grad_out))
         return bs_fail(s, BS_ERR_INVALID_ARG, "bad adjoint arguments");

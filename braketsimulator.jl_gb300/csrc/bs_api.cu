@@ -42,12 +42,50 @@ int bs_ensure_plan(bs_sim* s, int64_t bytes) {
 namespace {
 
 __global__ void k_basis0(double2* psi) { psi[0] = make_double2(1.0, 0.0); }
+__global__ void k_basis0_c64(float2* psi) { psi[0] = make_float2(1.0f, 0.0f); }
+
+// complex128 <-> complex64 element conversion (round to nearest)
+__global__ void k_to_c64(const double2* __restrict__ in, float2* __restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = make_float2(__double2float_rn(in[i].x), __double2float_rn(in[i].y));
+}
+__global__ void k_to_c128(const float2* __restrict__ in, double2* __restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = make_double2((double)in[i].x, (double)in[i].y);
+}
+
+int elem_bytes(const bs_sim* s) { return s->precision == BS_PREC_C64 ? 8 : 16; }
+
+// complex128 host buffer <-> complex64 state, through a bounded device staging buffer
+int transfer_c64(bs_sim* s, double* host, int64_t n, bool to_device) {
+    const int64_t chunk = std::min<int64_t>(n, (int64_t)1 << 22);   // 64 MiB of complex128
+    int rc = bs_ensure_scratch(s, chunk * 16);
+    if (rc) return rc;
+    double2* stage = (double2*)s->scratch;
+    float2* st = (float2*)s->state;
+    for (int64_t off = 0; off < n; off += chunk) {
+        const int64_t m = std::min<int64_t>(chunk, n - off);
+        const int blocks = (int)std::min<int64_t>((m + 255) / 256, 152 * 8);
+        if (to_device) {
+            rc = bs_cuda_check(s, cudaMemcpyAsync(stage, host + 2 * off, (size_t)m * 16, cudaMemcpyHostToDevice, s->stream), "set_state");
+            if (rc) return rc;
+            k_to_c64<<<blocks, 256, 0, s->stream>>>(stage, st + off, m);
+        } else {
+            k_to_c128<<<blocks, 256, 0, s->stream>>>(st + off, stage, m);
+            rc = bs_cuda_check(s, cudaMemcpyAsync(host + 2 * off, stage, (size_t)m * 16, cudaMemcpyDeviceToHost, s->stream), "get_state");
+            if (rc) return rc;
+        }
+        rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "state transfer");
+        if (rc) return rc;
+    }
+    return BS_OK;
+}
 
 int alloc_state(bs_sim* s, int n) {
     const int bits = (s->kind == BS_KIND_DM) ? 2 * n : n;
     if (n < 0 || bits > 34) return bs_fail(s, BS_ERR_INVALID_ARG, "qubit count out of range");
     const int64_t len = (int64_t)1 << bits;
-    const int64_t bytes = len * 16;
+    const int64_t bytes = len * elem_bytes(s);
     if (bytes > s->cap_bytes) {
         if (s->state) cudaFree(s->state);
         s->state = nullptr;
@@ -61,7 +99,8 @@ int alloc_state(bs_sim* s, int n) {
     s->alias_valid = false;
     int rc = bs_cuda_check(s, cudaMemsetAsync(s->state, 0, (size_t)bytes, s->stream), "state clear");
     if (rc) return rc;
-    k_basis0<<<1, 1, 0, s->stream>>>((double2*)s->state);
+    if (s->precision == BS_PREC_C64) k_basis0_c64<<<1, 1, 0, s->stream>>>((float2*)s->state);
+    else k_basis0<<<1, 1, 0, s->stream>>>((double2*)s->state);
     return bs_cuda_check(s, cudaGetLastError(), "state init");
 }
 
@@ -77,7 +116,7 @@ int bs_create(int kind, int n_qubits, int precision, bs_sim** out) {
     if (!out) return BS_ERR_INVALID_ARG;
     *out = nullptr;
     if (kind != BS_KIND_SV && kind != BS_KIND_DM) return BS_ERR_INVALID_ARG;
-    if (precision != BS_PREC_C128) return BS_ERR_UNSUPPORTED;
+    if (precision != BS_PREC_C128 && precision != BS_PREC_C64) return BS_ERR_INVALID_ARG;
     bs_sim* s = new (std::nothrow) bs_sim();
     if (!s) return BS_ERR_ALLOC;
     s->kind = kind;
@@ -124,6 +163,7 @@ int bs_set_state(bs_sim* s, const double* host, int64_t n) {
     if (!s) return BS_ERR_INVALID_ARG;
     if (!host || n != s->len) return bs_fail(s, BS_ERR_INVALID_ARG, "state length mismatch");
     s->alias_valid = false;
+    if (s->precision == BS_PREC_C64) return transfer_c64(s, const_cast<double*>(host), n, true);
     int rc = bs_cuda_check(s, cudaMemcpyAsync(s->state, host, (size_t)n * 16, cudaMemcpyHostToDevice, s->stream), "set_state");
     if (rc) return rc;
     return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "set_state sync");
@@ -132,6 +172,7 @@ int bs_set_state(bs_sim* s, const double* host, int64_t n) {
 int bs_get_state(bs_sim* s, double* host, int64_t n) {
     if (!s) return BS_ERR_INVALID_ARG;
     if (!host || n != s->len) return bs_fail(s, BS_ERR_INVALID_ARG, "state length mismatch");
+    if (s->precision == BS_PREC_C64) return transfer_c64(s, host, n, false);
     int rc = bs_cuda_check(s, cudaMemcpyAsync(host, s->state, (size_t)n * 16, cudaMemcpyDeviceToHost, s->stream), "get_state");
     if (rc) return rc;
     return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "get_state sync");
@@ -141,21 +182,23 @@ int bs_set_state_device(bs_sim* s, const void* dev, int64_t n) {
     if (!s) return BS_ERR_INVALID_ARG;
     if (!dev || n != s->len) return bs_fail(s, BS_ERR_INVALID_ARG, "state length mismatch");
     s->alias_valid = false;
-    return bs_cuda_check(s, cudaMemcpyAsync(s->state, dev, (size_t)n * 16, cudaMemcpyDeviceToDevice, s->stream), "set_state_device");
+    return bs_cuda_check(s, cudaMemcpyAsync(s->state, dev, (size_t)n * elem_bytes(s), cudaMemcpyDeviceToDevice, s->stream), "set_state_device");
 }
 
 int bs_get_state_device(bs_sim* s, void* dev, int64_t n) {
     if (!s) return BS_ERR_INVALID_ARG;
     if (!dev || n != s->len) return bs_fail(s, BS_ERR_INVALID_ARG, "state length mismatch");
-    return bs_cuda_check(s, cudaMemcpyAsync(dev, s->state, (size_t)n * 16, cudaMemcpyDeviceToDevice, s->stream), "get_state_device");
+    return bs_cuda_check(s, cudaMemcpyAsync(dev, s->state, (size_t)n * elem_bytes(s), cudaMemcpyDeviceToDevice, s->stream), "get_state_device");
 }
 
 int bs_copy_state(bs_sim* dst, const bs_sim* src) {
     if (!dst || !src) return BS_ERR_INVALID_ARG;
-    if (dst->kind != src->kind || dst->len != src->len) return bs_fail(dst, BS_ERR_INVALID_ARG, "simulators differ in kind or size");
+    if (dst->kind != src->kind || dst->len != src->len || dst->precision != src->precision)
+        return bs_fail(dst, BS_ERR_INVALID_ARG, "simulators differ in kind, size or precision");
     cudaStreamSynchronize(src->stream);
     dst->alias_valid = false;
-    return bs_cuda_check(dst, cudaMemcpyAsync(dst->state, src->state, (size_t)dst->len * 16, cudaMemcpyDeviceToDevice, dst->stream), "copy_state");
+    return bs_cuda_check(dst, cudaMemcpyAsync(dst->state, src->state, (size_t)dst->len * elem_bytes(dst),
+                                              cudaMemcpyDeviceToDevice, dst->stream), "copy_state");
 }
 
 int bs_synchronize(bs_sim* s) {

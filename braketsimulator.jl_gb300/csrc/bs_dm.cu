@@ -20,8 +20,15 @@ __device__ __forceinline__ double2 cmulDc(double2 a, double2 b) {   // a * conj(
     return make_double2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
 
-template <int K>
-__global__ void k_kraus_ref(double2* __restrict__ S, int n, const int* __restrict__ eb, const double2* __restrict__ kr, int nk) {
+__device__ __forceinline__ double2 to_d2(double2 v) { return v; }
+__device__ __forceinline__ double2 to_d2(float2 v) { return make_double2(v.x, v.y); }
+template <typename ST> __device__ __forceinline__ ST from_d2(double2 v);
+template <> __device__ __forceinline__ double2 from_d2<double2>(double2 v) { return v; }
+template <> __device__ __forceinline__ float2 from_d2<float2>(double2 v) { return make_float2((float)v.x, (float)v.y); }
+
+// ST: storage type of the density matrix (double2 for complex128, float2 for complex64)
+template <int K, typename ST>
+__global__ void k_kraus_ref(ST* __restrict__ S, int n, const int* __restrict__ eb, const double2* __restrict__ kr, int nk) {
     constexpr int D = 1 << K;
     const int64_t dim = (int64_t)1 << n;
     const int64_t nblk = dim >> K;
@@ -44,7 +51,7 @@ __global__ void k_kraus_ref(double2* __restrict__ S, int n, const int* __restric
         }
         double2 rho[D][D], acc[D][D];
         for (int i = 0; i < D; i++)
-            for (int j = 0; j < D; j++) { rho[i][j] = S[idx[i] + idx[j] * dim]; acc[i][j] = make_double2(0, 0); }
+            for (int j = 0; j < D; j++) { rho[i][j] = to_d2(S[idx[i] + idx[j] * dim]); acc[i][j] = make_double2(0, 0); }
         for (int q = 0; q < nk; q++) {
             const double2* Kq = kr + (int64_t)q * D * D;
             double2 t[D][D];
@@ -62,12 +69,13 @@ __global__ void k_kraus_ref(double2* __restrict__ S, int n, const int* __restric
                 }
         }
         for (int i = 0; i < D; i++)
-            for (int j = 0; j < D; j++) S[idx[i] + idx[j] * dim] = acc[i][j];
+            for (int j = 0; j < D; j++) S[idx[i] + idx[j] * dim] = from_d2<ST>(acc[i][j]);
     }
 }
 
 // k >= 3: one CTA per block, the D x D block and a work copy in shared memory
-__global__ void k_kraus_ref_big(double2* __restrict__ S, int n, int k, const int* __restrict__ eb,
+template <typename ST>
+__global__ void k_kraus_ref_big(ST* __restrict__ S, int n, int k, const int* __restrict__ eb,
                                 const double2* __restrict__ kr, int nk) {
     extern __shared__ double2 sm[];
     const int D = 1 << k;
@@ -96,7 +104,7 @@ __global__ void k_kraus_ref_big(double2* __restrict__ S, int n, int k, const int
     __syncthreads();
     for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
         int i = e / D, j = e % D;
-        rho[e] = S[idx[i] + idx[j] * dim];
+        rho[e] = to_d2(S[idx[i] + idx[j] * dim]);
         acc[e] = make_double2(0, 0);
     }
     __syncthreads();
@@ -119,7 +127,7 @@ __global__ void k_kraus_ref_big(double2* __restrict__ S, int n, int k, const int
     }
     for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
         int i = e / D, j = e % D;
-        S[idx[i] + idx[j] * dim] = acc[e];
+        S[idx[i] + idx[j] * dim] = from_d2<ST>(acc[e]);
     }
 }
 
@@ -153,20 +161,25 @@ int bs_kraus_reference(bs_sim* s, const double* kraus, int nk, int k, const int*
     if (rc) return rc;
     const int* d_eb = (const int*)s->plan_buf;
     const double2* d_k = (const double2*)((char*)s->plan_buf + 256);
-    double2* S = (double2*)s->state;
     const int64_t nblk = ((int64_t)1 << s->n) >> k;
     const int threads = 128;
     const int blocks = (int)std::min<int64_t>((nblk + threads - 1) / threads, 152 * 16);
-    switch (k) {
-        case 1: k_kraus_ref<1><<<blocks, threads, 0, s->stream>>>(S, s->n, d_eb, d_k, nk); break;
-        case 2: k_kraus_ref<2><<<blocks, threads, 0, s->stream>>>(S, s->n, d_eb, d_k, nk); break;
-        default: {
-            size_t sm = (size_t)3 * D * D * sizeof(double2) + (size_t)D * sizeof(int64_t);
-            if (sm > 200 * 1024) return bs_fail(s, BS_ERR_UNSUPPORTED, "channel too large");
-            cudaFuncSetAttribute(k_kraus_ref_big, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            k_kraus_ref_big<<<(unsigned)nblk, 256, sm, s->stream>>>(S, s->n, k, d_eb, d_k, nk);
+    auto run = [&](auto* S) -> int {
+        using ST = std::remove_pointer_t<decltype(S)>;
+        switch (k) {
+            case 1: k_kraus_ref<1, ST><<<blocks, threads, 0, s->stream>>>(S, s->n, d_eb, d_k, nk); break;
+            case 2: k_kraus_ref<2, ST><<<blocks, threads, 0, s->stream>>>(S, s->n, d_eb, d_k, nk); break;
+            default: {
+                size_t sm = (size_t)3 * D * D * sizeof(double2) + (size_t)D * sizeof(int64_t);
+                if (sm > 200 * 1024) return bs_fail(s, BS_ERR_UNSUPPORTED, "channel too large");
+                cudaFuncSetAttribute(k_kraus_ref_big<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+                k_kraus_ref_big<ST><<<(unsigned)nblk, 256, sm, s->stream>>>(S, s->n, k, d_eb, d_k, nk);
+            }
         }
-    }
+        return BS_OK;
+    };
+    rc = (s->precision == BS_PREC_C64) ? run((float2*)s->state) : run((double2*)s->state);
+    if (rc) return rc;
     s->stats.kernel_launches++;
     return bs_cuda_check(s, cudaGetLastError(), "kraus launch");
 }

@@ -73,6 +73,23 @@ __device__ __forceinline__ double2 store_c128(const cff& v) {
     return make_double2(ff2d(v.rh, v.rl), ff2d(v.ih, v.il));
 }
 
+// Storage policy: complex128 (double2) or complex64 (float2) amplitudes, read into the
+// float-float form used by reductions.  A float is exactly h with l = 0, so products
+// and sums of complex64 inputs are carried at FP64-level accuracy.
+template <bool C64> struct Elem;
+template <> struct Elem<false> {
+    using T = double2;
+    static __device__ __forceinline__ cff load(const T& v) { return load_c128(v); }
+    static __device__ __forceinline__ T store(const cff& c) { return store_c128(c); }
+};
+template <> struct Elem<true> {
+    using T = float2;
+    static __device__ __forceinline__ cff load(const T& v) { return {v.x, 0.f, v.y, 0.f}; }
+    static __device__ __forceinline__ T store(const cff& c) {
+        return make_float2(__fadd_rn(c.rh, c.rl), __fadd_rn(c.ih, c.il));
+    }
+};
+
 // ---------------------------------------------------------------- accumulation
 // Sum of exact products: s carries the running sum of the leading products with
 // every rounding error recovered by TwoSum; c collects the error terms and the

@@ -93,6 +93,9 @@ int bs_lower_gate(bs_sim* s, const double* matrix, int k, const int* targets, in
 int bs_lower_kraus_physical(bs_sim* s, const double* kraus, int nk, int k, const int* targets,
                             unsigned flags, std::vector<HostGate>& out);
 void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, std::vector<Sweep>& out);
+// Tile geometry: tile bits (10..12, env BS_TILE_BITS) and threads per CTA (256/512, env BS_TILE_THREADS)
+int bs_tile_bits();
+int bs_tile_threads();
 
 // ---- execution (bs_tile.cu)
 int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps);

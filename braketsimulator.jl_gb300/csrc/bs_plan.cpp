@@ -174,11 +174,29 @@ int bs_lower_kraus_physical(bs_sim* s, const double* kraus, int nk, int k, const
     return BS_OK;
 }
 
+int bs_tile_bits() {
+    static const int v = [] {
+        const char* e = getenv("BS_TILE_BITS");
+        int b = e ? atoi(e) : BS_TILE_MAX_BITS;
+        return (b >= 10 && b <= BS_TILE_MAX_BITS) ? b : BS_TILE_MAX_BITS;
+    }();
+    return v;
+}
+
+int bs_tile_threads() {
+    static const int v = [] {
+        const char* e = getenv("BS_TILE_THREADS");
+        int t = e ? atoi(e) : 256;
+        return (t == 512) ? 512 : 256;
+    }();
+    return v;
+}
+
 // Greedy sweep planner.  A gate may move ahead of gates it does not share a bit
 // with; a dense or monomial gate needs its target bits inside the tile, a
 // diagonal gate or a control never does (their bits are read from the index).
 void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, std::vector<Sweep>& out) {
-    const int T = std::min(BS_TILE_MAX_BITS, n_bits);
+    const int T = std::min(bs_tile_bits(), n_bits);
     const int L = std::min(BS_TILE_LOW_BITS, T);
     const int cap = T - L;
     const size_t G = gates.size();

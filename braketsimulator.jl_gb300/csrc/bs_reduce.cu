@@ -7,7 +7,8 @@
 // marginal_probability src/result_types.jl:96-113.
 // The reference copies the whole state and re-sweeps it per observable factor;
 // here each Pauli term is one pair-read of the state and terms that flip the same
-// bits share the read.
+// bits share the read.  Every kernel is templated on the storage (complex128 or
+// complex64); sums are carried in float-float, i.e. at FP64-level accuracy.
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -20,20 +21,26 @@ namespace {
 constexpr int kRThreads = 256;
 constexpr int kMaxTermsPerPass = 8;
 
-__global__ void k_prob_sv(const double2* __restrict__ psi, double* __restrict__ out, int64_t n) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        cff x = load_c128(psi[i]);
-        ffacc a;
-        acc_first(a, x.rh, x.rl, x.rh, x.rl);
-        acc_add(a, x.ih, x.il, x.ih, x.il);
-        ff r = acc_done(a);
-        out[i] = ff2d(r.h, r.l);
-    }
+template <bool C64>
+__device__ __forceinline__ double prob_of(const typename Elem<C64>::T& v) {
+    cff x = Elem<C64>::load(v);
+    ffacc a;
+    acc_first(a, x.rh, x.rl, x.rh, x.rl);
+    acc_add(a, x.ih, x.il, x.ih, x.il);
+    ff r = acc_done(a);
+    return ff2d(r.h, r.l);
 }
 
-__global__ void k_prob_dm(const double2* __restrict__ S, double* __restrict__ out, int64_t dim) {
+template <bool C64>
+__global__ void k_prob_sv(const typename Elem<C64>::T* __restrict__ psi, double* __restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = prob_of<C64>(psi[i]);
+}
+
+template <bool C64>
+__global__ void k_prob_dm(const typename Elem<C64>::T* __restrict__ S, double* __restrict__ out, int64_t dim) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = S[i * (dim + 1)].x;
+        out[i] = (double)S[i * (dim + 1)].x;
 }
 
 struct TermSet {
@@ -43,7 +50,7 @@ struct TermSet {
     int slot[kMaxTermsPerPass];       // output slot
 };
 
-// block reduction of per-thread doubles into partial[blockIdx.x * stride + slot]
+// block reduction of per-thread doubles into partial[idx]
 __device__ void block_sum_store(double v, double* partial, int64_t idx) {
     __shared__ double red[kRThreads / 32];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -58,10 +65,27 @@ __device__ void block_sum_store(double v, double* partial, int64_t idx) {
     }
 }
 
+__device__ __forceinline__ void pauli_accumulate(ffsum* acc, const TermSet& ts, int64_t i, float wrh, float wrl,
+                                                 float wih, float wil) {
+    for (int t = 0; t < ts.nt; t++) {
+        bool neg = __popcll((unsigned long long)i & ts.zm[t]) & 1;
+        float vh, vl;
+        switch (ts.ph[t]) {            // Re((-i)^ph * w)
+            case 0: vh = wrh; vl = wrl; break;
+            case 1: vh = wih; vl = wil; break;
+            case 2: vh = -wrh; vl = -wrl; break;
+            default: vh = -wih; vl = -wil; break;
+        }
+        if (neg) { vh = -vh; vl = -vl; }
+        fsum_add(acc[t], vh, vl);
+    }
+}
+
 // SV Pauli terms sharing flip mask xm.  Pairs (i, i^xm) with the top bit of xm
 // clear contribute 2 Re(c(i) conj(psi_i) psi_{i^xm}); xm == 0 gives |psi_i|^2 * sign.
-__global__ void __launch_bounds__(kRThreads) k_pauli_sv(const double2* __restrict__ psi, int64_t n, uint64_t xm,
-                                                        TermSet ts, double* __restrict__ partial, int n_slots) {
+template <bool C64>
+__global__ void __launch_bounds__(kRThreads) k_pauli_sv(const typename Elem<C64>::T* __restrict__ psi, int64_t n,
+                                                        uint64_t xm, TermSet ts, double* __restrict__ partial, int n_slots) {
     ffsum acc[kMaxTermsPerPass];
     for (int t = 0; t < kMaxTermsPerPass; t++) acc[t] = {0.f, 0.f};
     const int64_t npairs = xm ? n / 2 : n;
@@ -69,10 +93,10 @@ __global__ void __launch_bounds__(kRThreads) k_pauli_sv(const double2* __restric
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npairs; p += (int64_t)gridDim.x * blockDim.x) {
         int64_t i = p;
         if (xm) { int64_t low = p & ((1LL << hb) - 1); i = ((p >> hb) << (hb + 1)) | low; }
-        cff a = load_c128(psi[i]);
+        cff a = Elem<C64>::load(psi[i]);
         float wrh, wrl, wih, wil;
         if (xm) {
-            cff b = load_c128(psi[i ^ (int64_t)xm]);
+            cff b = Elem<C64>::load(psi[i ^ (int64_t)xm]);
             ffacc r, m;
             acc_first(r, a.rh, a.rl, b.rh, b.rl);
             acc_add(r, a.ih, a.il, b.ih, b.il);
@@ -87,42 +111,21 @@ __global__ void __launch_bounds__(kRThreads) k_pauli_sv(const double2* __restric
             ff rr = acc_done(r);
             wrh = rr.h; wrl = rr.l; wih = 0.f; wil = 0.f;
         }
-        for (int t = 0; t < ts.nt; t++) {
-            bool neg = __popcll((unsigned long long)i & ts.zm[t]) & 1;
-            float vh, vl;
-            switch (ts.ph[t]) {            // Re((-i)^ph * w)
-                case 0: vh = wrh; vl = wrl; break;
-                case 1: vh = wih; vl = wil; break;
-                case 2: vh = -wrh; vl = -wrl; break;
-                default: vh = -wih; vl = -wil; break;
-            }
-            if (neg) { vh = -vh; vl = -vl; }
-            fsum_add(acc[t], vh, vl);
-        }
+        pauli_accumulate(acc, ts, i, wrh, wrl, wih, wil);
     }
     for (int t = 0; t < ts.nt; t++)
         block_sum_store(ff2d(acc[t].h, acc[t].l), partial, (int64_t)blockIdx.x * n_slots + ts.slot[t]);
 }
 
 // DM Pauli terms: E = sum_a Re(P[a, a^xm] S[a, a^xm]), S[r, c] at r + c*dim.
-__global__ void __launch_bounds__(kRThreads) k_pauli_dm(const double2* __restrict__ S, int64_t dim, uint64_t xm,
-                                                        TermSet ts, double* __restrict__ partial, int n_slots) {
+template <bool C64>
+__global__ void __launch_bounds__(kRThreads) k_pauli_dm(const typename Elem<C64>::T* __restrict__ S, int64_t dim,
+                                                        uint64_t xm, TermSet ts, double* __restrict__ partial, int n_slots) {
     ffsum acc[kMaxTermsPerPass];
     for (int t = 0; t < kMaxTermsPerPass; t++) acc[t] = {0.f, 0.f};
     for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < dim; a += (int64_t)gridDim.x * blockDim.x) {
-        cff v = load_c128(S[a + (a ^ (int64_t)xm) * dim]);
-        for (int t = 0; t < ts.nt; t++) {
-            bool neg = __popcll((unsigned long long)a & ts.zm[t]) & 1;
-            float vh, vl;
-            switch (ts.ph[t]) {
-                case 0: vh = v.rh; vl = v.rl; break;
-                case 1: vh = v.ih; vl = v.il; break;
-                case 2: vh = -v.rh; vl = -v.rl; break;
-                default: vh = -v.ih; vl = -v.il; break;
-            }
-            if (neg) { vh = -vh; vl = -vl; }
-            fsum_add(acc[t], vh, vl);
-        }
+        cff v = Elem<C64>::load(S[a + (a ^ (int64_t)xm) * dim]);
+        pauli_accumulate(acc, ts, a, v.rh, v.rl, v.ih, v.il);
     }
     for (int t = 0; t < ts.nt; t++)
         block_sum_store(ff2d(acc[t].h, acc[t].l), partial, (int64_t)blockIdx.x * n_slots + ts.slot[t]);
@@ -152,11 +155,15 @@ __global__ void k_sum_partials(const double* __restrict__ partial, int nblocks, 
 __device__ __forceinline__ double2 cmulD(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+template <bool C64>
+__device__ __forceinline__ double2 ld2(const typename Elem<C64>::T& v) { return make_double2((double)v.x, (double)v.y); }
 
 // <O> for a k-target matrix (FP64): SV sum_g x^H O x, DM sum_g sum_ab O[a,b] S[(a,g),(b,g)]
-__global__ void __launch_bounds__(kRThreads) k_matrix_expect(const double2* __restrict__ st, int nbits_q, int k,
-                                                             const int* __restrict__ eb, const double2* __restrict__ O,
-                                                             int dm, double* __restrict__ partial) {
+template <bool C64>
+__global__ void __launch_bounds__(kRThreads) k_matrix_expect(const typename Elem<C64>::T* __restrict__ st, int nbits_q,
+                                                             int k, const int* __restrict__ eb,
+                                                             const double2* __restrict__ O, int dm,
+                                                             double* __restrict__ partial) {
     const int D = 1 << k;
     const int64_t dim = (int64_t)1 << nbits_q;
     const int64_t ngroups = dim >> k;
@@ -175,18 +182,17 @@ __global__ void __launch_bounds__(kRThreads) k_matrix_expect(const double2* __re
         for (int a = 0; a < D; a++) {
             int64_t ia = p;
             for (int q = 0; q < k; q++) if ((a >> q) & 1) ia |= 1LL << eb[q];
-            double2 xa = dm ? make_double2(0, 0) : st[ia];
+            double2 xa = dm ? make_double2(0, 0) : ld2<C64>(st[ia]);
             for (int b = 0; b < D; b++) {
                 int64_t ib = p;
                 for (int q = 0; q < k; q++) if ((b >> q) & 1) ib |= 1LL << eb[q];
                 double2 o = O[a * D + b];
                 if (dm) {
-                    double2 v = cmulD(o, st[ia + ib * dim]);
+                    double2 v = cmulD(o, ld2<C64>(st[ia + ib * dim]));
                     acc += v.x;
                 } else {
-                    double2 xb = st[ib];
-                    double2 v = cmulD(o, xb);          // O[a,b] x_b
-                    acc += xa.x * v.x + xa.y * v.y;    // Re(conj(x_a) * v)
+                    double2 v = cmulD(o, ld2<C64>(st[ib]));   // O[a,b] x_b
+                    acc += xa.x * v.x + xa.y * v.y;           // Re(conj(x_a) * v)
                 }
             }
         }
@@ -196,25 +202,17 @@ __global__ void __launch_bounds__(kRThreads) k_matrix_expect(const double2* __re
 
 // marginal probabilities: out[o] = sum of p_i over i whose target bits spell o
 // (output bit j <-> j-th smallest endian target bit)
-__global__ void __launch_bounds__(kRThreads) k_marginal(const double2* __restrict__ st, int dm, int nbits_q, int k,
-                                                        const int* __restrict__ eb_sorted, double* __restrict__ partial) {
+template <bool C64>
+__global__ void __launch_bounds__(kRThreads) k_marginal(const typename Elem<C64>::T* __restrict__ st, int dm, int nbits_q,
+                                                        int k, const int* __restrict__ eb_sorted,
+                                                        double* __restrict__ partial) {
     extern __shared__ double hist[];
     const int D = 1 << k;
     const int64_t dim = (int64_t)1 << nbits_q;
     for (int o = threadIdx.x; o < D; o += blockDim.x) hist[o] = 0.0;
     __syncthreads();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x) {
-        double p;
-        if (dm) {
-            p = st[i * (dim + 1)].x;
-        } else {
-            cff x = load_c128(st[i]);
-            ffacc a;
-            acc_first(a, x.rh, x.rl, x.rh, x.rl);
-            acc_add(a, x.ih, x.il, x.ih, x.il);
-            ff r = acc_done(a);
-            p = ff2d(r.h, r.l);
-        }
+        double p = dm ? (double)st[i * (dim + 1)].x : prob_of<C64>(st[i]);
         int o = 0;
         for (int q = 0; q < k; q++) o |= (int)((i >> eb_sorted[q]) & 1) << q;
         atomicAdd(&hist[o], p);
@@ -228,6 +226,15 @@ int grid_for(int64_t work) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 8));
 }
 
+template <bool C64>
+void launch_pauli(bs_sim* s, int nb, int64_t dim, uint64_t xm, const TermSet& set, double* partial, int n_terms) {
+    using T = typename Elem<C64>::T;
+    if (s->kind == BS_KIND_SV)
+        k_pauli_sv<C64><<<nb, kRThreads, 0, s->stream>>>((const T*)s->state, dim, xm, set, partial, n_terms);
+    else
+        k_pauli_dm<C64><<<nb, kRThreads, 0, s->stream>>>((const T*)s->state, dim, xm, set, partial, n_terms);
+}
+
 }  // namespace
 
 extern "C" {
@@ -239,8 +246,14 @@ int bs_probabilities(bs_sim* s, double* host_out, int64_t n) {
     int rc = bs_ensure_scratch(s, dim * 8);
     if (rc) return rc;
     double* d = (double*)s->scratch;
-    if (s->kind == BS_KIND_SV) k_prob_sv<<<grid_for(dim), kRThreads, 0, s->stream>>>((const double2*)s->state, d, dim);
-    else k_prob_dm<<<grid_for(dim), kRThreads, 0, s->stream>>>((const double2*)s->state, d, dim);
+    const bool c64 = s->precision == BS_PREC_C64;
+    if (s->kind == BS_KIND_SV) {
+        if (c64) k_prob_sv<true><<<grid_for(dim), kRThreads, 0, s->stream>>>((const float2*)s->state, d, dim);
+        else k_prob_sv<false><<<grid_for(dim), kRThreads, 0, s->stream>>>((const double2*)s->state, d, dim);
+    } else {
+        if (c64) k_prob_dm<true><<<grid_for(dim), kRThreads, 0, s->stream>>>((const float2*)s->state, d, dim);
+        else k_prob_dm<false><<<grid_for(dim), kRThreads, 0, s->stream>>>((const double2*)s->state, d, dim);
+    }
     rc = bs_cuda_check(s, cudaMemcpyAsync(host_out, d, (size_t)dim * 8, cudaMemcpyDeviceToHost, s->stream), "probabilities");
     if (rc) return rc;
     return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "probabilities sync");
@@ -272,8 +285,7 @@ int bs_expectation_pauli(bs_sim* s, int n_terms, const uint64_t* xmask, const ui
         groups[xe].push_back(t);
     }
     const int64_t dim = (int64_t)1 << n;
-    const int64_t work = (s->kind == BS_KIND_SV) ? dim : dim;
-    const int nb = grid_for(work);
+    const int nb = grid_for(dim);
     int rc = bs_ensure_scratch(s, ((int64_t)nb * n_terms + n_terms) * 8);
     if (rc) return rc;
     double* partial = (double*)s->scratch;
@@ -291,10 +303,8 @@ int bs_expectation_pauli(bs_sim* s, int n_terms, const uint64_t* xmask, const ui
                 set.ph[j] = ph[t];
                 set.slot[j] = t;
             }
-            if (s->kind == BS_KIND_SV)
-                k_pauli_sv<<<nb, kRThreads, 0, s->stream>>>((const double2*)s->state, dim, kv.first, set, partial, n_terms);
-            else
-                k_pauli_dm<<<nb, kRThreads, 0, s->stream>>>((const double2*)s->state, dim, kv.first, set, partial, n_terms);
+            if (s->precision == BS_PREC_C64) launch_pauli<true>(s, nb, dim, kv.first, set, partial, n_terms);
+            else launch_pauli<false>(s, nb, dim, kv.first, set, partial, n_terms);
         }
     }
     k_sum_partials<<<n_terms, 256, 0, s->stream>>>(partial, nb, n_terms, res);
@@ -335,8 +345,13 @@ int bs_expectation_matrix(bs_sim* s, const double* matrix, int k, const int* tar
     rc = bs_cuda_check(s, cudaMemcpyAsync(s->plan_buf, host.data(), host.size(), cudaMemcpyHostToDevice, s->stream), "observable upload");
     if (rc) return rc;
     double* partial = (double*)s->scratch;
-    k_matrix_expect<<<nb, kRThreads, 0, s->stream>>>((const double2*)s->state, s->n, k, (const int*)s->plan_buf,
-                                                      (const double2*)((char*)s->plan_buf + 256), s->kind == BS_KIND_DM, partial);
+    const int* d_eb = (const int*)s->plan_buf;
+    const double2* d_o = (const double2*)((char*)s->plan_buf + 256);
+    const int dm = s->kind == BS_KIND_DM;
+    if (s->precision == BS_PREC_C64)
+        k_matrix_expect<true><<<nb, kRThreads, 0, s->stream>>>((const float2*)s->state, s->n, k, d_eb, d_o, dm, partial);
+    else
+        k_matrix_expect<false><<<nb, kRThreads, 0, s->stream>>>((const double2*)s->state, s->n, k, d_eb, d_o, dm, partial);
     k_sum_partials<<<1, 256, 0, s->stream>>>(partial, nb, 1, partial + nb);
     rc = bs_cuda_check(s, cudaMemcpyAsync(out, partial + nb, 8, cudaMemcpyDeviceToHost, s->stream), "expectation");
     if (rc) return rc;
@@ -365,8 +380,11 @@ int bs_marginal_probabilities(bs_sim* s, int k, const int* targets, double* host
     rc = bs_cuda_check(s, cudaMemcpyAsync(s->plan_buf, eb.data(), sizeof(int) * (size_t)k, cudaMemcpyHostToDevice, s->stream), "marginal upload");
     if (rc) return rc;
     double* partial = (double*)s->scratch;
-    k_marginal<<<nb, kRThreads, (size_t)D * 8, s->stream>>>((const double2*)s->state, s->kind == BS_KIND_DM, s->n, k,
-                                                             (const int*)s->plan_buf, partial);
+    const int dm = s->kind == BS_KIND_DM;
+    if (s->precision == BS_PREC_C64)
+        k_marginal<true><<<nb, kRThreads, (size_t)D * 8, s->stream>>>((const float2*)s->state, dm, s->n, k, (const int*)s->plan_buf, partial);
+    else
+        k_marginal<false><<<nb, kRThreads, (size_t)D * 8, s->stream>>>((const double2*)s->state, dm, s->n, k, (const int*)s->plan_buf, partial);
     k_sum_partials<<<D, 256, 0, s->stream>>>(partial, nb, D, partial + (int64_t)nb * D);
     rc = bs_cuda_check(s, cudaMemcpyAsync(host_out, partial + (int64_t)nb * D, (size_t)D * 8, cudaMemcpyDeviceToHost, s->stream), "marginal");
     if (rc) return rc;

@@ -24,9 +24,12 @@ namespace {
 
 constexpr int kBlk = 4096;        // probabilities per CDF block
 
-__device__ __forceinline__ double prob_at(const double2* st, int dm, int64_t dim, int64_t i) {
-    if (dm) return st[i * (dim + 1)].x;
-    cff x = load_c128(st[i]);
+// mode bit 0: density matrix (diagonal of the stored matrix); bit 1: complex64 storage
+__device__ __forceinline__ double prob_at(const double2* st, int mode, int64_t dim, int64_t i) {
+    const float2* st32 = reinterpret_cast<const float2*>(st);
+    const bool c64 = (mode & 2) != 0;
+    if (mode & 1) return c64 ? (double)st32[i * (dim + 1)].x : st[i * (dim + 1)].x;
+    cff x = c64 ? Elem<true>::load(st32[i]) : load_c128(st[i]);
     ffacc a;
     acc_first(a, x.rh, x.rl, x.rh, x.rl);
     acc_add(a, x.ih, x.il, x.ih, x.il);
@@ -176,7 +179,7 @@ int build_cdf(bs_sim* s, double** incl_out, int64_t* nb_out) {
     if (rc) return rc;
     double* bsum = (double*)s->scratch;
     double* incl = bsum + nb;
-    k_block_sums<<<(unsigned)nb, 256, 0, s->stream>>>((const double2*)s->state, s->kind == BS_KIND_DM, dim, bsum);
+    k_block_sums<<<(unsigned)nb, 256, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, bsum);
     k_scan_blocks<<<1, 1024, 0, s->stream>>>(bsum, nb, incl);
     *incl_out = incl;
     *nb_out = nb;
@@ -239,7 +242,7 @@ int bs_alias_build(bs_sim* s, double wsum, unsigned flags) {
     rc = bs_ensure_scratch(s, 3 * dim * 8 + 128);
     if (rc) return rc;
     double* p = (double*)s->scratch;
-    k_prob_any<<<grid(dim, 256), 256, 0, s->stream>>>((const double2*)s->state, s->kind == BS_KIND_DM, dim, p);
+    k_prob_any<<<grid(dim, 256), 256, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, p);
     return alias_from_device_probs(s, p, dim, wsum);
 }
 
@@ -306,7 +309,7 @@ int bs_sample_direct(bs_sim* s, const double* u, int64_t shots, double wsum, int
     int64_t* dout = (int64_t*)(du + shots);
     cudaMemcpyAsync(du, u, (size_t)shots * 8, cudaMemcpyHostToDevice, s->stream);
     const int64_t dim = (int64_t)1 << s->n;
-    k_sample_direct<<<grid(shots, 128), 128, 0, s->stream>>>((const double2*)s->state, s->kind == BS_KIND_DM, dim, incl, nb,
+    k_sample_direct<<<grid(shots, 128), 128, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, incl, nb,
                                                                du, wsum, shots, dout);
     cudaMemcpyAsync(out, dout, (size_t)shots * 8, cudaMemcpyDeviceToHost, s->stream);
     cudaFreeAsync(buf, s->stream);
@@ -326,7 +329,7 @@ int bs_sample(bs_sim* s, uint64_t seed, int64_t shots, int64_t* out) {
     if (rc) return rc;
     int64_t* dout = (int64_t*)buf;
     const int64_t dim = (int64_t)1 << s->n;
-    k_sample_rng<<<grid(shots, 128), 128, 0, s->stream>>>((const double2*)s->state, s->kind == BS_KIND_DM, dim, incl, nb,
+    k_sample_rng<<<grid(shots, 128), 128, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, incl, nb,
                                                             seed, shots, dout);
     cudaMemcpyAsync(out, dout, (size_t)shots * 8, cudaMemcpyDeviceToHost, s->stream);
     cudaFreeAsync(buf, s->stream);

@@ -86,13 +86,16 @@ def _ops_for(instructions, dm: bool, noise_mode: int):
     return arr, len(ops), keep
 
 
+PRECISIONS = {"c128": _abi.BS_PREC_C128, "c64": _abi.BS_PREC_C64}
+
+
 class _Handle:
     """Owns one engine handle (bs_sim*)."""
 
-    def __init__(self, kind: int, n: int):
+    def __init__(self, kind: int, n: int, precision: str = "c128"):
         self._lib = _abi.lib()
         h = C.c_void_p()
-        rc = self._lib.bs_create(kind, n, _abi.BS_PREC_C128, C.byref(h))
+        rc = self._lib.bs_create(kind, n, PRECISIONS[precision], C.byref(h))
         if rc != 0:
             raise _abi.BraketGB300Error(rc, "bs_create failed")
         self.h = h
@@ -115,11 +118,14 @@ class _Handle:
 class AbstractSimulator:
     kind = _abi.BS_KIND_SV
 
-    def __init__(self, qubit_count: int, shots: int = 0, noise_mode: str = "reference"):
+    def __init__(self, qubit_count: int, shots: int = 0, noise_mode: str = "reference", precision: str = "c128"):
+        """precision "c128" (complex128 state) or "c64" (complex64 state, FP32 gate arithmetic,
+        probabilities / expectations / sampling still accumulated at FP64 accuracy)."""
         self.qubit_count = int(qubit_count)
         self.shots = int(shots)
         self.noise_mode = noise_mode
-        self._h = _Handle(self.kind, self.qubit_count)
+        self.precision = precision
+        self._h = _Handle(self.kind, self.qubit_count, precision)
         self._obs = None
         self.seed = 0
 
@@ -133,7 +139,7 @@ class AbstractSimulator:
         return self
 
     def similar(self, shots: int | None = None):
-        return type(self)(self.qubit_count, self.shots if shots is None else shots, self.noise_mode)
+        return type(self)(self.qubit_count, self.shots if shots is None else shots, self.noise_mode, self.precision)
 
     def copy(self):
         s = self.similar()

@@ -56,6 +56,35 @@ def test_deep_layers(n):
     assert st["sweeps"] < len(ops)   # gates were fused into tiles
 
 
+@pytest.mark.parametrize("n", [12, 16, 21])
+def test_one_target_sweeps_with_controls_and_diagonals(n):
+    """Sweeps whose non-diagonal gates are all 1-target (the register-blocked kernel's domain):
+    in-tile and out-of-tile controls, negated controls, monomials and diagonals on far qubits."""
+    rng = np.random.default_rng(n + 100)
+    ops = []
+    for _ in range(80):
+        q = int(rng.integers(n))
+        r = int(rng.integers(6))
+        if r == 0:
+            a = rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2))
+            ops.append(bs.Instruction(bs.Unitary(np.linalg.qr(a)[0]), [q]))
+        elif r == 1:
+            ops.append(bs.Instruction([bs.H(), bs.Rx(0.3), bs.Ry(-1.2), bs.V(), bs.S(), bs.T()][rng.integers(6)], [q]))
+        elif r == 2:
+            c = int(rng.choice([x for x in range(n) if x != q]))
+            ops.append(bs.Instruction(bs.CNot(), [c, q]))
+        elif r == 3:
+            c1, c2 = [int(x) for x in rng.choice([x for x in range(n) if x != q], 2, replace=False)]
+            ops.append(bs.Instruction(bs.Control(bs.U(0.4, 0.2, -0.7), (0, 1)), [c1, c2, q]))
+        elif r == 4:
+            c = int(rng.choice([x for x in range(n) if x != q]))
+            ops.append(bs.Instruction([bs.CZ(), bs.CPhaseShift(0.7), bs.ZZ(0.2)][rng.integers(3)], [c, q]))
+        else:
+            ops.append(bs.Instruction(bs.Rz(float(rng.normal())), [q]))
+    sim = bs.StateVectorSimulator(n, 0).evolve(ops)
+    assert rel_err(sim.state_vector, oracle.OracleSV(n).evolve(ops).psi) < TOL
+
+
 def test_ghz10():
     ops = [bs.Instruction(bs.H(), [0])] + [bs.Instruction(bs.CNot(), [0, k]) for k in range(1, 10)]
     sim = bs.StateVectorSimulator(10, 1000).evolve(ops)
