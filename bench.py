@@ -276,6 +276,59 @@ def dm_bench(bs, n=14):
     return out
 
 
+def batch_circuits(bs, nc=512, seed=7):
+    """512 circuits: qubits U{12..26}, depth U{10..60} layers of ceil(n/2) gates from
+    {H, Rx, Ry, Rz, CNOT, CZ, Swap, CCNot} on seeded random qubits; 8 Pauli strings each."""
+    rng = np.random.default_rng(seed)
+    circuits, counts, obs = [], [], []
+    for _ in range(nc):
+        n = int(rng.integers(12, 27))
+        depth = int(rng.integers(10, 61))
+        ins = []
+        for _ in range(depth * ((n + 1) // 2)):
+            r = int(rng.integers(8))
+            q = [int(x) for x in rng.choice(n, 3, replace=False)]
+            if r == 0:
+                ins.append(bs.Instruction(bs.H(), [q[0]]))
+            elif r in (1, 2, 3):
+                ins.append(bs.Instruction([bs.Rx, bs.Ry, bs.Rz][r - 1](float(rng.uniform(-np.pi, np.pi))), [q[0]]))
+            elif r == 4:
+                ins.append(bs.Instruction(bs.CNot(), q[:2]))
+            elif r == 5:
+                ins.append(bs.Instruction(bs.CZ(), q[:2]))
+            elif r == 6:
+                ins.append(bs.Instruction(bs.Swap(), q[:2]))
+            else:
+                ins.append(bs.Instruction(bs.CCNot(), q))
+        terms = [{int(t): "XYZ"[rng.integers(3)] for t in rng.choice(n, int(rng.integers(1, 5)), replace=False)}
+                 for _ in range(8)]
+        circuits.append(ins)
+        counts.append(n)
+        obs.append(terms)
+    return circuits, counts, obs
+
+
+def batch_bench(bs):
+    import torch
+    circuits, counts, obs = batch_circuits(bs)
+    bs.batch_simulate(circuits[:8], counts[:8], obs[:8], shots=1000, seed=1)      # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    exp, smp, st = bs.batch_simulate(circuits, counts, obs, shots=1000, seed=2, precision="c64")
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    # error of the complex64 run against complex128 on a few circuits (the smallest ones)
+    small = sorted(range(len(counts)), key=lambda c: counts[c])[:4]
+    e128, _, _ = bs.batch_simulate([circuits[c] for c in small], [counts[c] for c in small], [obs[c] for c in small],
+                                   shots=0, precision="c128")
+    err = float(np.max(np.abs(exp[small] - e128)))
+    return {"circuits": len(circuits), "qubits": "12..26", "gates": int(sum(len(c) for c in circuits)),
+            "shots_each": 1000, "expectations_each": 8, "precision": "c64 (FP64 reductions)",
+            "s_per_batch": round(dt, 3), "circuits_per_s": round(len(circuits) / dt, 1),
+            "device_ms": round(st["gpu_ms"], 1), "sweeps": st["sweeps"],
+            "max_abs_err_c64_vs_c128_expectations": err}
+
+
 def run_reference(args, rank, world):
     """--impl reference: the reference's CPU kernels (oracle port; Julia is not installed)
     on the host cores, bounded sample of the same workload per step."""
@@ -384,6 +437,7 @@ def main():
         line["adjoint"] = adjoint_bench(bs)
         line["ghz10"] = ghz_bench(bs)
         line["dm14"] = dm_bench(bs)
+        line["batch512"] = batch_bench(bs)
     print(json.dumps(line), flush=True)
 
 

@@ -87,6 +87,8 @@ SIGNATURES = {
     "bs_adjoint_gradient": (_i32, [_p, _P(BsOp), _i64, _P(C.c_int32), _P(C.c_int32), _P(_u64), _P(_u64),
                                    _i32, _i32, _P(_u64), _P(_u64), _P(_f64), _P(_f64), _P(_f64)]),
     "bs_expectation_pauli_noalloc": (_i32, [_p, _i32, _i32, _i32, _P(_u64), _P(_u64), _P(_f64), _P(_f64), _p]),
+    "bs_run_batch": (_i32, [_i32, _P(_i32), _P(_P(BsOp)), _P(_i64), _i32, _P(_u64), _P(_u64), _i64, _u64, _i32,
+                            _P(_f64), _P(_i64), _P(BsStats)]),
     "bs_synchronize": (_i32, [_p]),
     "bs_state_device_ptr": (_i32, [_p, _P(_p)]),
 }

@@ -25,6 +25,10 @@ struct TileGate {
     uint64_t gc_mask, gc_val;
     int32_t mat_off;            // offset (in cff units) into the sweep's matrix pool
     int32_t perm_off;           // monomial: offset into the permutation pool (int32 pairs)
+    // kind 3: a run of CZ gates as one phase (-1)^(sum_q popc(i & (i >> pshift[q]) & pmask[q]))
+    int32_t npar;
+    int32_t pshift[4];
+    uint64_t pmask[4];
 };
 
 struct SweepDesc {

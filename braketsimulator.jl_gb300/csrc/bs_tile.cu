@@ -125,6 +125,14 @@ __device__ void tile_monomial(float4* sm, int T, const TileGate& g, const int32_
     }
 }
 
+// phase of a merged run of CZ gates at global index gi: odd parity -> -1
+__device__ __forceinline__ bool parity_odd(const TileGate& g, int64_t gi) {
+    int par = 0;
+    for (int q = 0; q < g.npar; q++)
+        par ^= __popcll((unsigned long long)(gi & (gi >> g.pshift[q])) & g.pmask[q]);
+    return par & 1;
+}
+
 __device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const float4* __restrict__ mats,
                           int64_t base, const int64_t* off_tab) {
     const int nt = 1 << T, lowmask = (1 << L) - 1;
@@ -179,7 +187,12 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
         const TileGate& g = d.gates[gi];
         if ((base & (int64_t)g.gc_mask) != (int64_t)g.gc_val) continue;   // uniform in the CTA
         const int kind = g.kind, k = g.k;
-        if (kind == 1) {
+        if (kind == 3) {
+            for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+                const int64_t gi = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+                if (parity_odd(g, gi)) { float4 v = smem[j]; smem[j] = make_float4(-v.x, -v.y, -v.z, -v.w); }
+            }
+        } else if (kind == 1) {
             tile_diag(smem, T, L, g, d.mats, base, off_tab);
         } else if (kind == 0) {
             if (k == 1) tile_dense<1>(smem, T, g, d.mats);
@@ -389,7 +402,12 @@ __global__ void __launch_bounds__(kThreads) k_tile_sweep_c64(float2* __restrict_
         const TileGate& g = d.gates[gi];
         if ((base & (int64_t)g.gc_mask) != (int64_t)g.gc_val) continue;
         const int kind = g.kind, k = g.k;
-        if (kind == 1) {
+        if (kind == 3) {
+            for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+                const int64_t gi = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+                if (parity_odd(g, gi)) { float2 v = smem[j]; smem[j] = make_float2(-v.x, -v.y); }
+            }
+        } else if (kind == 1) {
             tile_diag_c64(smem, T, L, g, d.mats, base, off_tab);
         } else if (kind == 0) {
             if (k == 1) tile_dense_c64<1>(smem, T, g, d.mats);
@@ -632,6 +650,7 @@ std::vector<RBSeg> rb_segments(const std::vector<TileGate>& tg, int64_t g0, int 
     if (T != 12) return segs;
     for (int i = 0; i < ng; i++) {
         const TileGate& g = tg[(size_t)(g0 + i)];
+        if (g.kind == 3) return {};
         if (g.kind == 1) { if (g.k > BS_TILE_MAXK) return {}; continue; }
         if (g.k != 1 || g.tbit[0] < 0) return {};
     }
@@ -701,6 +720,29 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         for (int b = 0; b < L; b++) local[b] = b;
         for (size_t i = 0; i < sw.hi_bits.size(); i++) local[sw.hi_bits[i]] = L + (int)i;
         for (const HostGate& hg : sw.gates) {
+            // consecutive CZ gates (Z on one bit, one control at value 1) merge into one parity-phase gate
+            if (hg.kind == 1 && hg.k == 1 && hg.mat.size() == 4 && hg.mat[0] == 1.0 && hg.mat[1] == 0.0 &&
+                hg.mat[2] == -1.0 && hg.mat[3] == 0.0 && __builtin_popcountll(hg.cmask) == 1 && hg.cval == hg.cmask) {
+                const int c = 63 - __builtin_clzll(hg.cmask), t = hg.ebit[0];
+                const int lo = std::min(c, t), dd = std::max(c, t) - lo;
+                auto add_pair = [&](TileGate& g) {
+                    for (int q = 0; q < g.npar; q++)
+                        if (g.pshift[q] == dd) { g.pmask[q] ^= 1ULL << lo; return true; }   // CZ twice = identity
+                    if (g.npar == 4) return false;
+                    g.pshift[g.npar] = dd;
+                    g.pmask[g.npar] = 1ULL << lo;
+                    g.npar++;
+                    return true;
+                };
+                if (!(ln.n_gates > 0 && tg.back().kind == 3 && add_pair(tg.back()))) {
+                    TileGate t3{};
+                    t3.kind = 3;
+                    add_pair(t3);
+                    tg.push_back(t3);
+                    ln.n_gates++;
+                }
+                continue;
+            }
             bool big = hg.kind != 1 && hg.k > BS_TILE_MAXK;
             if (!big && hg.kind != 1)
                 for (int q = 0; q < hg.k; q++) if (local[hg.ebit[q]] < 0) big = true;

@@ -183,6 +183,15 @@ int bs_expectation_pauli_noalloc(const void* state_dev, int kind, int n_qubits, 
                                  const uint64_t* xmask, const uint64_t* zmask, const double* coeffs,
                                  double* out, void* stream);
 
+/* ---- batched simulate (src/BraketSimulator.jl:347-395): n_circuits independent circuits, each
+ * from |0...0> on n_qubits[c] qubits with ops[c][0..n_ops[c]).  Returns per circuit n_terms Pauli
+ * expectations (term t of circuit c at xmask/zmask[c*n_terms + t], bit q <-> qubit q) and `shots`
+ * basis-index samples.  Circuits of <= 12 qubits (complex64) run whole in one CTA each inside one
+ * persistent launch; larger ones run as tile sweeps on a pool of streams.  No handle needed. */
+int bs_run_batch(int n_circuits, const int* n_qubits, const bs_op* const* ops, const int64_t* n_ops,
+                 int n_terms, const uint64_t* xmask, const uint64_t* zmask, int64_t shots, uint64_t seed,
+                 int precision, double* expectations_out, int64_t* samples_out, bs_stats* stats_out);
+
 /* synchronise the handle's stream; device pointer of the state (for in-HBM benchmarking) */
 int bs_synchronize(bs_sim* sim);
 int bs_state_device_ptr(bs_sim* sim, void** out);
