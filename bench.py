@@ -387,7 +387,7 @@ def main():
     for i in range(args.warmup):
         step(bs, sim, ops, SHOTS, 100 + i)
     barrier()
-    dev_ms, bytes_moved, sweeps, launches = 0.0, 0.0, 0, 0
+    dev_ms, bytes_moved, sweeps, launches, tc_gates = 0.0, 0.0, 0, 0, 0
     with Clocks(local) as clk:
         t0 = time.perf_counter()
         for i in range(args.steps):
@@ -396,6 +396,7 @@ def main():
             bytes_moved += st["bytes_moved"]
             sweeps += st["sweeps"]
             launches += st["kernel_launches"]
+            tc_gates += st["tc_gates"]
         barrier()
         wall = time.perf_counter() - t0
     if world > 1:
@@ -426,6 +427,7 @@ def main():
                      "frac": round(achieved / hbm, 3), "traffic": None, "peak_source": src,
                      "kernel": "k_tile_sweep", "bytes_per_launch": 32 * 2 ** N_QUBITS},
         "gate_layer": {"sweeps_per_step": sweeps // args.steps, "gates_per_step": n_gates,
+                       "tensor_core_fused_unitaries_per_step": tc_gates // args.steps,
                        "gate_equivalent_GBps": round(gate_eq, 1),
                        "layer_ms": round(dev_ms / args.steps / (2 * LAYERS), 2)},
         "gpu_launches": int(launches),

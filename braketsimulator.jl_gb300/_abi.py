@@ -54,6 +54,7 @@ class BsStats(C.Structure):
         ("gates", C.c_int64),
         ("bytes_moved", C.c_double),
         ("gpu_ms", C.c_double),
+        ("tc_gates", C.c_int64),
     ]
 
 

@@ -137,6 +137,7 @@ int bs_destroy(bs_sim* s) {
     if (s->state) cudaFree(s->state);
     if (s->scratch) cudaFree(s->scratch);
     if (s->plan_buf) cudaFree(s->plan_buf);
+    if (s->dev_flag) cudaFree(s->dev_flag);
     if (s->alias_ap) cudaFree(s->alias_ap);
     if (s->alias_ix) cudaFree(s->alias_ix);
     if (s->ev0) cudaEventDestroy(s->ev0);
@@ -203,7 +204,8 @@ int bs_copy_state(bs_sim* dst, const bs_sim* src) {
 
 int bs_synchronize(bs_sim* s) {
     if (!s) return BS_ERR_INVALID_ARG;
-    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "synchronize");
+    int rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "synchronize");
+    return rc ? rc : bs_check_device_flag(s);
 }
 
 int bs_state_device_ptr(bs_sim* s, void** out) {
@@ -303,7 +305,7 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     float ms = 0;
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);
     s->stats.gpu_ms = ms;
-    return BS_OK;
+    return bs_check_device_flag(s);
 }
 
 }  // extern "C"

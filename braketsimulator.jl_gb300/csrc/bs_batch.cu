@@ -327,6 +327,7 @@ extern "C" int bs_run_batch(int n_circuits, const int* n_qubits, const bs_op* co
                 wst[(size_t)w].kernel_launches += h->stats.kernel_launches;
                 wst[(size_t)w].gates += h->stats.gates;
                 wst[(size_t)w].bytes_moved += h->stats.bytes_moved;
+                wst[(size_t)w].tc_gates += h->stats.tc_gates;
             }
             if (!r && n_terms)
                 r = bs_expectation_pauli(h, n_terms, xmask + (size_t)c * n_terms, zmask + (size_t)c * n_terms, nullptr,
@@ -349,6 +350,7 @@ extern "C" int bs_run_batch(int n_circuits, const int* n_qubits, const bs_op* co
         tot.kernel_launches += x.kernel_launches;
         tot.gates += x.gates;
         tot.bytes_moved += x.bytes_moved;
+        tot.tc_gates += x.tc_gates;
     }
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);

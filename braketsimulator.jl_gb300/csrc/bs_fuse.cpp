@@ -1,0 +1,307 @@
+// Gate fusion for the tensor-core tile path.
+//
+// Inside one tile sweep, runs of gates are folded into dense unitaries on 5
+// tile bits.  A gate can join a block when its dense targets lie in the tile and
+// its tile bits fit the block; bits outside the tile (controls, and target bits
+// of diagonal gates) are constant within a CTA, so the block is built once per
+// assignment of those "uniform" bits (at most 3 of them) and each CTA picks its
+// variant.  The products are formed here in FP64; the device applies them to the
+// tile as real 64x64 GEMMs on tcgen05 tensor cores, with both operands split
+// into exact 8-bit bf16 digits (an Ozaki-style split) so that the result keeps
+// float-float accuracy.  This replaces, for those gates, the per-gate amplitude
+// loops of the reference (src/gate_kernels.jl:489-775, src/custom_gates.jl:364-416);
+// the fused product itself has no counterpart there.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdlib>
+#include <cstring>
+#include "bs_internal.h"
+
+namespace {
+
+using cd = std::complex<double>;
+constexpr int kMaxUniform = 3;
+
+// cost of a gate on the float-float path, in units of one dense 1-qubit gate
+double ff_cost(const HostGate& g) {
+    if (g.kind == 0) return (double)(1 << g.k) / 2.0;
+    if (g.kind == 2) return 0.25;
+    return 0.3;
+}
+
+bool is_plain_cz(const HostGate& g) {
+    return g.kind == 1 && g.k == 1 && g.mat.size() == 4 && g.mat[0] == 1.0 && g.mat[1] == 0.0 && g.mat[2] == -1.0 &&
+           g.mat[3] == 0.0 && __builtin_popcountll(g.cmask) == 1 && g.cval == g.cmask;
+}
+
+// Apply a canonical gate to a 32-amplitude vector over the block bits.  pos[e]: block bit of
+// endian bit e, or -1 for a uniform bit whose value is (uval >> e) & 1.
+void apply_block(const HostGate& g, const int* pos, uint64_t uval, cd* v) {
+    // controls: in-block ones become an index condition, uniform ones decide whether the gate acts
+    uint32_t cm = 0, cv = 0;
+    for (int e = 0; e < 64; e++) {
+        if (!((g.cmask >> e) & 1ULL)) continue;
+        const uint64_t want = (g.cval >> e) & 1ULL;
+        if (pos[e] < 0) {
+            if (((uval >> e) & 1ULL) != want) return;
+        } else {
+            cm |= 1u << pos[e];
+            cv |= (uint32_t)want << pos[e];
+        }
+    }
+    const int D = 1 << g.k;
+    if (g.kind == 1) {
+        // diagonal: target bits may be uniform (constant over the block)
+        for (uint32_t i = 0; i < 32; i++) {
+            if ((i & cm) != cv) continue;
+            int di = 0;
+            for (int q = 0; q < g.k; q++) {
+                const int e = g.ebit[q];
+                const int bit = pos[e] >= 0 ? (int)((i >> pos[e]) & 1u) : (int)((uval >> e) & 1ULL);
+                di |= bit << q;
+            }
+            v[i] *= cd(g.mat[2 * di], g.mat[2 * di + 1]);
+        }
+        return;
+    }
+    int tb[BS_MAX_TARGETS];
+    uint32_t tmask = 0;
+    for (int q = 0; q < g.k; q++) { tb[q] = pos[g.ebit[q]]; tmask |= 1u << tb[q]; }
+    auto dep = [&](int c) {
+        uint32_t j = 0;
+        for (int q = 0; q < g.k; q++) if ((c >> q) & 1) j |= 1u << tb[q];
+        return j;
+    };
+    for (uint32_t i = 0; i < 32; i++) {
+        if (i & tmask) continue;
+        if ((i & cm) != cv) continue;
+        cd x[32], y[32];
+        for (int c = 0; c < D; c++) x[c] = v[i | dep(c)];
+        if (g.kind == 0) {
+            for (int r = 0; r < D; r++) {
+                cd s = 0;
+                for (int c = 0; c < D; c++) s += cd(g.mat[2 * (r * D + c)], g.mat[2 * (r * D + c) + 1]) * x[c];
+                y[r] = s;
+            }
+        } else {
+            static const cd ipow[4] = {cd(1, 0), cd(0, 1), cd(-1, 0), cd(0, -1)};
+            for (int c = 0; c < D; c++) y[g.perm[2 * c]] = ipow[g.perm[2 * c + 1] & 3] * x[c];
+        }
+        for (int r = 0; r < D; r++) v[i | dep(r)] = y[r];
+    }
+}
+
+struct Block {
+    uint64_t bits = 0;               // tile bits touched
+    uint64_t ubits = 0;              // uniform (out-of-tile) bits the gates depend on
+    std::vector<int> idx;            // gate indices, in order
+    double cost = 0;
+};
+
+double tc_cost() {
+    const char* v = getenv("BS_TC_COST");
+    return v ? atof(v) : 2.0;
+}
+
+}  // namespace
+
+// BS_TC=0 keeps every gate on the float-float path (read on every call, so a process can compare both)
+bool bs_tc_enabled() {
+    const char* v = getenv("BS_TC");
+    return !(v && v[0] == '0');
+}
+
+void bs_fuse_tc(const std::vector<HostGate>& in, const int* local, int T, std::vector<HostGate>& out) {
+    out.clear();
+    const double threshold = tc_cost();
+    std::vector<Block> open;
+    auto emit = [&](Block& b) {
+        int ndense = 0;
+        bool wide = false;   // 3- and 4-target gates always fuse: the tensor-core sweep has no float-float path for them
+        for (int i : b.idx) {
+            ndense += in[(size_t)i].kind == 0;
+            wide = wide || (in[(size_t)i].kind != 1 && in[(size_t)i].k >= 3);
+        }
+        if (!wide && (b.cost <= threshold || ndense == 0)) {
+            for (int i : b.idx) out.push_back(in[(size_t)i]);
+            return;
+        }
+        // block bits ascending by tile position, padded to 5 with other tile bits (high ones first, so that
+        // the low contiguous bits stay column bits of the GEMM where possible)
+        std::vector<int> eb;
+        for (int e = 0; e < 64; e++) if ((b.bits >> e) & 1ULL) eb.push_back(e);
+        std::vector<int> tile_e(T, -1);
+        for (int e = 0; e < 64; e++) if (local[e] >= 0 && local[e] < T) tile_e[local[e]] = e;
+        for (int p = T - 1; p >= 0 && (int)eb.size() < 5; p--) {
+            int e = tile_e[p];
+            if (e >= 0 && !((b.bits >> e) & 1ULL)) eb.push_back(e);
+        }
+        std::sort(eb.begin(), eb.end(), [&](int a, int c) { return local[a] < local[c]; });
+        int pos[64];
+        for (int e = 0; e < 64; e++) pos[e] = -1;
+        for (int q = 0; q < 5; q++) pos[eb[(size_t)q]] = q;
+        HostGate f;
+        f.kind = 4;
+        f.k = 5;
+        for (int q = 0; q < 5; q++) f.ebit[q] = eb[(size_t)q];
+        for (int e = 0; e < 64; e++) if ((b.ubits >> e) & 1ULL) f.ubits.push_back(e);
+        const int nvar = 1 << f.ubits.size();
+        f.mat.assign((size_t)nvar * 2 * 32 * 32, 0.0);
+        for (int var = 0; var < nvar; var++) {
+            uint64_t uval = 0;
+            for (size_t i = 0; i < f.ubits.size(); i++) if ((var >> i) & 1) uval |= 1ULL << f.ubits[i];
+            double* m = f.mat.data() + (size_t)var * 2048;
+            for (int c = 0; c < 32; c++) {
+                cd v[32];
+                for (int r = 0; r < 32; r++) v[r] = 0;
+                v[c] = 1;
+                for (int i : b.idx) apply_block(in[(size_t)i], pos, uval, v);
+                for (int r = 0; r < 32; r++) {
+                    m[2 * (r * 32 + c)] = v[r].real();
+                    m[2 * (r * 32 + c) + 1] = v[r].imag();
+                }
+            }
+        }
+        out.push_back(std::move(f));
+    };
+    auto flush_if = [&](uint64_t bits) {
+        for (size_t j = 0; j < open.size();) {
+            if (open[j].bits & bits) {
+                emit(open[j]);
+                open.erase(open.begin() + (long)j);
+            } else {
+                j++;
+            }
+        }
+    };
+    for (size_t i = 0; i < in.size(); i++) {
+        const HostGate& g = in[i];
+        // tile bits and uniform bits of the gate; dense and monomial targets must be in the tile
+        uint64_t bits = 0, ub = 0;
+        bool fusable = g.kind <= 2 && g.k <= 5;
+        for (int q = 0; q < g.k; q++) {
+            const int e = g.ebit[q];
+            if (local[e] >= 0) bits |= 1ULL << e;
+            else if (g.kind == 1) ub |= 1ULL << e;
+            else fusable = false;
+        }
+        for (int e = 0; e < 64; e++)
+            if ((g.cmask >> e) & 1ULL) {
+                if (local[e] >= 0) bits |= 1ULL << e;
+                else ub |= 1ULL << e;
+            }
+        if (__builtin_popcountll(bits) > 5 || __builtin_popcountll(ub) > kMaxUniform || bits == 0) fusable = false;
+        if (!fusable) {
+            // close every block sharing a bit with the gate, uniform bits included (the gate may act on them)
+            const uint64_t all = bits | ub | g.cmask;
+            uint64_t tgt = 0;
+            for (int q = 0; q < g.k; q++) tgt |= 1ULL << g.ebit[q];
+            for (size_t j = 0; j < open.size();) {
+                if ((open[j].bits | open[j].ubits) & (all | tgt)) {
+                    emit(open[j]);
+                    open.erase(open.begin() + (long)j);
+                } else {
+                    j++;
+                }
+            }
+            out.push_back(g);
+            continue;
+        }
+        const double gc = is_plain_cz(g) ? 0.1 : ff_cost(g);
+        uint64_t uni = bits, uu = ub;
+        for (const Block& b : open) if (b.bits & bits) { uni |= b.bits; uu |= b.ubits; }
+        if (__builtin_popcountll(uni) > 5 || __builtin_popcountll(uu) > kMaxUniform) {
+            // the gate links blocks that cannot all merge: keep the costliest block it fits into and close
+            // the others (their gates precede it and touch none of the kept block's tile bits)
+            int keep = -1;
+            for (size_t j = 0; j < open.size(); j++)
+                if ((open[j].bits & bits) && __builtin_popcountll(open[j].bits | bits) <= 5 &&
+                    __builtin_popcountll(open[j].ubits | ub) <= kMaxUniform &&
+                    (keep < 0 || open[j].cost > open[(size_t)keep].cost))
+                    keep = (int)j;
+            if (keep >= 0) {
+                const uint64_t kb = open[(size_t)keep].bits;
+                for (size_t j = 0; j < open.size();) {
+                    if ((open[j].bits & bits) && open[j].bits != kb) {
+                        emit(open[j]);
+                        open.erase(open.begin() + (long)j);
+                    } else {
+                        j++;
+                    }
+                }
+                for (const Block& b : open) if (b.bits == kb) { uni = kb | bits; uu = b.ubits | ub; }
+            }
+        }
+        if (__builtin_popcountll(uni) <= 5 && __builtin_popcountll(uu) <= kMaxUniform) {
+            Block nb;
+            nb.bits = uni;
+            nb.ubits = uu;
+            // merge the intersecting blocks (pairwise disjoint in tile bits, so their gates commute)
+            for (size_t j = 0; j < open.size();) {
+                if (open[j].bits & bits) {
+                    nb.idx.insert(nb.idx.end(), open[j].idx.begin(), open[j].idx.end());
+                    nb.cost += open[j].cost;
+                    open.erase(open.begin() + (long)j);
+                } else {
+                    j++;
+                }
+            }
+            std::sort(nb.idx.begin(), nb.idx.end());
+            nb.idx.push_back((int)i);
+            nb.cost += gc;
+            open.push_back(std::move(nb));
+        } else {
+            flush_if(bits);
+            Block nb;
+            nb.bits = bits;
+            nb.ubits = ub;
+            nb.idx.push_back((int)i);
+            nb.cost = gc;
+            open.push_back(std::move(nb));
+        }
+    }
+    for (Block& b : open) emit(b);
+}
+
+bool bs_tc_exponent(const double* mat, int n_mat, int& eu) {
+    double mx = 0;
+    for (size_t i = 0; i < (size_t)n_mat * 2048; i++) {
+        if (!std::isfinite(mat[i])) return false;
+        mx = std::max(mx, std::fabs(mat[i]));
+    }
+    int e = 0;
+    if (mx > 0) std::frexp(mx, &e);          // mx < 2^e
+    if (e > 12) return false;
+    eu = std::max(e, -60);
+    return true;
+}
+
+bool bs_tc_digits(const double* mat, uint16_t* dst, int eu) {
+    // real embedding: n = 2 t' + c' (output re/im), k = 2 t + c (input re/im); entries below 2^eu
+    std::vector<double> ur(64 * 64);
+    for (int tp = 0; tp < 32; tp++)
+        for (int t = 0; t < 32; t++) {
+            const double re = mat[2 * (tp * 32 + t)], im = mat[2 * (tp * 32 + t) + 1];
+            ur[(2 * tp) * 64 + 2 * t] = re;
+            ur[(2 * tp) * 64 + 2 * t + 1] = -im;
+            ur[(2 * tp + 1) * 64 + 2 * t] = im;
+            ur[(2 * tp + 1) * 64 + 2 * t + 1] = re;
+        }
+    // six balanced digits d_i in [-128, 128]: u 2^(7-eu) = sum_i d_i 2^(-8 i); slice i holds d_i 2^(-8 i) as bf16
+    for (int n = 0; n < 64; n++)
+        for (int k = 0; k < 64; k++) {
+            double v = std::ldexp(ur[n * 64 + k], 7 - eu);
+            if (!(std::fabs(v) < 128.0)) return false;
+            for (int i = 0; i < 6; i++) {
+                const double d = std::nearbyint(v);
+                v = (v - d) * 256.0;
+                const float f = std::ldexp((float)d, -8 * i);   // exact: |d| <= 128
+                uint32_t bits;
+                std::memcpy(&bits, &f, 4);
+                const int s = k / 16, kc = (k % 16) / 8, rg = n / 8, r = n % 8, el = k % 8;
+                dst[(size_t)(i * 4 + s) * 1024 + rg * 128 + kc * 64 + r * 8 + el] = (uint16_t)(bits >> 16);
+            }
+        }
+    return true;
+}

@@ -14,6 +14,9 @@
 //   kind 0: dense 2^k x 2^k on tile-local bits tbit[0..k-1] (matrix bit j <-> tbit[j])
 //   kind 1: diagonal 2^k entries selected by global bits gbit[0..k-1]
 //   kind 2: monomial (one unit-modulus phase i^p per column) on tile-local bits
+//   kind 3: a run of CZ gates applied as one parity phase (npar, pshift, pmask)
+//   kind 4: fused dense unitary on 5 tile-local bits gbit[0..4] (matrix bit j <-> gbit[j]),
+//           applied on the tensor cores from the bf16 digit slices at tc_off (48 KiB blocks)
 // Controls: (tile_index & lc_mask) == lc_val for in-tile controls,
 //           (global_base & gc_mask) == gc_val for controls outside the tile.
 struct TileGate {
@@ -29,6 +32,10 @@ struct TileGate {
     int32_t npar;
     int32_t pshift[4];
     uint64_t pmask[4];
+    int32_t tc_off;             // kind 4: index of the digit-slice block in the sweep's pool
+    int32_t tc_eu;              // kind 4: matrix entries are below 2^tc_eu
+    int32_t tc_nu;              // kind 4: the CTA's base bits tc_ub[0..tc_nu-1] select the variant block
+    int32_t tc_ub[3];
 };
 
 struct SweepDesc {
@@ -41,15 +48,19 @@ struct SweepDesc {
     const TileGate* gates;      // device
     const float4* mats;         // device, complex float-float entries (rh, rl, ih, il)
     const int32_t* perms;       // device
+    const uint16_t* tc_pool;    // device, kind-4 digit slices (24576 bf16 per gate)
+    int* err;                   // device flag: a bounded tensor-core wait gave up
 };
 
 struct HostGate {                // a gate after lowering to the canonical convention
-    int kind;                    // 0 dense, 1 diagonal, 2 monomial
+    int kind;                    // 0 dense, 1 diagonal, 2 monomial, 4 fused 5-bit unitary
     int k;
     int ebit[BS_MAX_TARGETS];    // endian bit of target j (matrix bit j)
     std::vector<double> mat;     // interleaved complex; dense 4^k*2, diag 2^k*2
     uint64_t cmask = 0, cval = 0;// controls on endian bits
     std::vector<int> perm;       // monomial: column c -> (row, i-power)
+    std::vector<int> ubits;      // kind 4: out-of-tile bits the fused matrix depends on; mat holds
+                                 // 2^|ubits| matrices, variant v for bit values v_i at ubits[i]
 };
 
 struct Sweep {
@@ -77,6 +88,8 @@ struct bs_sim {
     void* plan_buf = nullptr;
     int64_t plan_bytes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int* dev_flag = nullptr;      // device error flag of the tensor-core sweeps
+    bool flag_armed = false;
     bs_stats stats{};
     std::string err;
 };
@@ -101,8 +114,21 @@ void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, std::vector<
 int bs_tile_bits();
 int bs_tile_threads();
 
+// ---- tensor-core fusion (bs_fuse.cpp)
+bool bs_tc_enabled();
+// Fold runs of in-tile gates into kind-4 HostGates (5 endian bits, 32x32 matrix) where that is cheaper.
+// local[e]: tile position of endian bit e or -1.
+void bs_fuse_tc(const std::vector<HostGate>& in, const int* local, int T, std::vector<HostGate>& out);
+// Six bf16 digit slices of the 64x64 real embedding of a 32x32 matrix, in the shared-memory
+// operand layout (24576 values); eu: entries are below 2^eu.  False if not representable.
+bool bs_tc_digits(const double* mat, uint16_t* dst, int eu);
+// Smallest eu with every entry of the n_mat 32x32 matrices below 2^eu; false if not finite or above 2^12.
+bool bs_tc_exponent(const double* mat, int n_mat, int& eu);
+
 // ---- execution (bs_tile.cu)
 int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps);
+// BS_ERR_TIMEOUT if a tensor-core sweep since the last check gave up on a bounded wait
+int bs_check_device_flag(bs_sim* s);
 
 // ---- reference-compat Kraus (bs_dm.cu)
 int bs_kraus_reference(bs_sim* s, const double* kraus, int nk, int k, const int* targets,

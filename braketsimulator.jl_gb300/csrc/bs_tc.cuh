@@ -1,0 +1,280 @@
+// Tensor-core application of a fused 5-bit unitary to a 2^12-amplitude tile.
+//
+// The tile (float-float complex values in shared memory) is viewed as 128
+// columns of 32 amplitudes: the 5 target bits index a column's amplitudes, the
+// other 7 tile bits index the column.  With the real embedding
+//     out[2t'+c'] = sum_k U_real[2t'+c'][k] x[k],  x[2t+0] = Re a_t, x[2t+1] = Im a_t
+// the gate is D[128 x 64] = A[128 x 64] * U_real^T, one tcgen05 GEMM per tile.
+//
+// Exactness (Ozaki-style split): every column is scaled by a power of two so
+// that |x| < 1, and both x (on the device) and U_real (on the host) are split
+// into six balanced 8-bit digits, digit j carried as bf16 d_j * 2^(-8j) with
+// |d_j| <= 128 (256 for the one digit that absorbs the float-float low word).
+// The 26 digit pairs with i + j <= 6 are accumulated in five rounds by digit
+// weight: i+j = 0, 1, 2, 3 each alone (every product a multiple of the same
+// power of two and every partial sum below 2^24 of it, so these FP32 sums are
+// exact) and i+j = 4, 5, 6 together (rounding at 2^-56 of the result).  After
+// each round the CUDA cores fold the FP32 accumulator into a running
+// float-float sum.  What remains is the 48-bit truncation of both operands,
+// ~2^-46 of the column's largest value per fused gate.
+//
+// TMEM (256 columns per CTA, so that two CTAs share an SM and one's MMAs
+// overlap the other's CUDA-core work):
+//   D (one FP32 accumulator, reused by the five rounds): columns 0..63, lane m.
+//   A (state digits): lanes 0..127 = columns m, TMEM columns kA0 + 32 j + t hold
+//     (Re, Im) of digit j of amplitude t as a bf16 pair (low half = Re).
+// B (matrix digits): shared memory, K-major, no swizzle: 8x8 core matrices of
+//   128 B; per (digit i, k-step s) a 2 KiB block, row groups 256 B apart (SBO),
+//   the two K halves 128 B apart (LBO).  Built on the host by bs_tc_digits.
+#pragma once
+#include <cstdint>
+
+namespace tc {
+
+constexpr int kA0 = 64;         // first TMEM column of the six A digit slices
+constexpr uint32_t kCols = 256; // TMEM columns held by one CTA
+// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, N = 64, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr long long kSpin = 1LL << 31;   // cycles before a wait gives up (~1 s)
+constexpr int kPoolBlock = 24576;        // bf16 values per fused matrix (6 digits x 64 x 64)
+
+// Bank swizzle of the 2^12 tile: bits 3..11 folded into bits 0..2, so that strided columns of
+// 16-byte values (any 5 target bits) spread over all bank groups.  A bijection on [0, 4096).
+__device__ __forceinline__ int sw(int j) { return j ^ (((j >> 3) ^ (j >> 6) ^ (j >> 9)) & 7); }
+
+__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start, LBO 128 B, SBO 256 B, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t bdesc(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+           (1ULL << 46);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// bounded wait for the phase with the given parity; false if it did not complete in kSpin cycles
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > kSpin) return false;
+    }
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t slot) {   // whole warp
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr) {   // whole warp
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(kCols));
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void st8(uint32_t taddr, const uint32_t (&w)[8]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(w[0]),
+                 "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7])
+                 : "memory");
+}
+__device__ __forceinline__ void ld8(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mma(uint32_t d, uint32_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d),
+        "r"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// Six digits of y = yh + yl (|y| < 2^7 after scaling): q[j] = d_j 2^(-8j), y ~ sum_j q[j].
+// Rounding to the digit grid uses the 1.5 * 2^(23-8j) shift, exact while |R| < 2^(22-8j).
+__device__ __forceinline__ void digits(float yh, float yl, float (&q)[6]) {
+    float R = yh;
+    q[0] = __fsub_rn(__fadd_rn(R, 12582912.0f), 12582912.0f);            // grid 1
+    R = __fsub_rn(R, q[0]);
+    q[1] = __fsub_rn(__fadd_rn(R, 49152.0f), 49152.0f);                  // grid 2^-8
+    R = __fsub_rn(R, q[1]);
+    q[2] = __fsub_rn(__fadd_rn(R, 192.0f), 192.0f);                      // grid 2^-16
+    R = __fadd_rn(__fsub_rn(R, q[2]), yl);                               // low word joins here
+    q[3] = __fsub_rn(__fadd_rn(R, 0.75f), 0.75f);                        // grid 2^-24
+    R = __fsub_rn(R, q[3]);
+    q[4] = __fsub_rn(__fadd_rn(R, 0.0029296875f), 0.0029296875f);        // grid 2^-32
+    R = __fsub_rn(R, q[4]);
+    q[5] = __fsub_rn(__fadd_rn(R, 1.1444091796875e-05f), 1.1444091796875e-05f);   // grid 2^-40
+}
+
+// error-free s + g (Knuth TwoSum): s <- rounded sum, returns the rounding error
+__device__ __forceinline__ float two_sum(float& s, float g) {
+    const float t = __fadd_rn(s, g);
+    const float bb = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(g, bb));
+    s = t;
+    return e;
+}
+
+struct State {
+    uint32_t tmem;       // TMEM base address
+    uint32_t bar_u;      // digit-slice copy completion
+    uint32_t bar_m;      // MMA completion
+    uint32_t ph_u, ph_m; // expected phase parities
+};
+
+// Thread 0: issue the MMAs of one digit-weight round into D, then commit to bar_m.
+__device__ __forceinline__ void issue_round(const State& st, uint32_t bB, int round) {
+    const int g0 = round < 4 ? round : 4, g1 = round < 4 ? round : 6;
+    bool first = true;
+    for (int gs = g0; gs <= g1; gs++)
+        for (int j = 0; j <= gs; j++) {
+            const int i = gs - j;
+            if (i > 5 || j > 5) continue;
+#pragma unroll
+            for (int s = 0; s < 4; s++) {
+                mma(st.tmem, st.tmem + (uint32_t)(kA0 + 32 * j + 8 * s), bdesc(bB + (uint32_t)((i * 4 + s) * 2048)),
+                    first ? 0u : 1u);
+                first = false;
+            }
+        }
+    commit(st.bar_m);
+}
+
+// Applies fused gate g to the (swizzled) 2^12 tile sm.  Called by all 256 threads of the CTA,
+// which then synchronise.  base: the CTA's global base index (selects the matrix variant).
+// On a wait that gives up, sets *fail and *err and leaves the tile partly updated.
+__device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint16_t* __restrict__ pool, uint16_t* sB,
+                                      State& st, int64_t base, uint8_t* s_emax, int* s_tpos, int* s_fail, int* err) {
+    const int tid = threadIdx.x, warp = tid >> 5, m = tid & 127, h = tid >> 7;
+    if (tid == 0) {
+        // the previous readers of sB (the MMAs of the previous fused gate) have completed
+        int var = 0;
+        for (int i = 0; i < g.tc_nu; i++) var |= (int)((base >> g.tc_ub[i]) & 1) << i;
+        mbar_expect_tx(st.bar_u, (uint32_t)kPoolBlock * 2);
+        const uint16_t* src = pool + (size_t)(g.tc_off + var) * kPoolBlock;
+        for (int i = 0; i < 6; i++) bulk_g2s(su32(sB) + (uint32_t)i * 8192u, src + i * 4096, 8192u, st.bar_u);
+    }
+    int tb[5];
+    uint32_t tmask = 0;
+#pragma unroll
+    for (int q = 0; q < 5; q++) { tb[q] = g.gbit[q]; tmask |= 1u << tb[q]; }
+    if (tid < 32) {
+        int p = 0;
+#pragma unroll
+        for (int q = 0; q < 5; q++) if ((tid >> q) & 1) p |= 1 << tb[q];
+        s_tpos[tid] = p;
+    }
+    int pm = 0;
+    for (int b = 0, src = 0; b < 12; b++)
+        if (!((tmask >> b) & 1u)) { pm |= ((m >> src) & 1) << b; src++; }
+    __syncthreads();
+    // column scale: largest exponent of the high words over the column (two threads per column)
+    uint32_t eb = 0;
+#pragma unroll 4
+    for (int a = 0; a < 16; a++) {
+        const float4 v = sm[sw(pm | s_tpos[16 * h + a])];
+        eb = max(eb, (__float_as_uint(v.x) >> 23) & 0xFFu);
+        eb = max(eb, (__float_as_uint(v.z) >> 23) & 0xFFu);
+    }
+    s_emax[tid] = (uint8_t)eb;
+    __syncthreads();
+    eb = max(eb, (uint32_t)s_emax[tid ^ 128]);
+    const int ebc = max((int)eb, max(6, 14 - g.tc_eu));
+    const float sc = __uint_as_float((uint32_t)(260 - ebc) << 23);                 // 2^(7 - E)
+    const float osc = __uint_as_float((uint32_t)(ebc - 13 + g.tc_eu) << 23);       // 2^(E + eu - 14)
+    const uint32_t lane = (uint32_t)((warp & 3) * 32) << 16;
+#pragma unroll 1
+    for (int c = 0; c < 2; c++) {
+        uint32_t w[6][8];
+#pragma unroll
+        for (int a = 0; a < 8; a++) {
+            const float4 v = sm[sw(pm | s_tpos[16 * h + 8 * c + a])];
+            float qr[6], qi[6];
+            digits(__fmul_rn(v.x, sc), __fmul_rn(v.y, sc), qr);
+            digits(__fmul_rn(v.z, sc), __fmul_rn(v.w, sc), qi);
+#pragma unroll
+            for (int j = 0; j < 6; j++) w[j][a] = __byte_perm(__float_as_uint(qr[j]), __float_as_uint(qi[j]), 0x7632);
+        }
+#pragma unroll
+        for (int j = 0; j < 6; j++) st8(st.tmem + lane + (uint32_t)(kA0 + 32 * j + 16 * h + 8 * c), w[j]);
+    }
+    wait_st();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t bB = su32(sB);
+    if (tid == 0) {
+        if (mbar_wait(st.bar_u, st.ph_u)) issue_round(st, bB, 0);
+        else { *s_fail = 1; atomicExch(err, 1); }
+    }
+    st.ph_u ^= 1u;
+    // running float-float sums of the thread's 32 outputs (16 amplitudes x re/im)
+    float s[32], e[32];
+#pragma unroll 1
+    for (int round = 0; round < 5; round++) {
+        if (tid == 0 && !*s_fail) {
+            if (!mbar_wait(st.bar_m, st.ph_m)) { *s_fail = 1; atomicExch(err, 1); }
+        }
+        st.ph_m ^= 1u;
+        __syncthreads();
+        if (*s_fail) return;
+        fence_after();
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            uint32_t r[8];
+            ld8(st.tmem + lane + (uint32_t)(32 * h + 8 * c), r);
+            wait_ld();
+#pragma unroll
+            for (int a = 0; a < 8; a++) {
+                const int o = 8 * c + a;
+                const float gv = __uint_as_float(r[a]);
+                if (round == 0) { s[o] = gv; e[o] = 0.f; }
+                else if (round <= 2) e[o] = __fadd_rn(e[o], two_sum(s[o], gv));
+                else e[o] = __fadd_rn(e[o], gv);
+            }
+        }
+        fence_before();
+        __syncthreads();
+        fence_after();
+        // D is free again: start the next round (the other CTA on the SM runs meanwhile)
+        if (round < 4 && tid == 0) issue_round(st, bB, round + 1);
+    }
+#pragma unroll
+    for (int a = 0; a < 16; a++) {
+        const int o = 2 * a;
+        float rh = __fadd_rn(s[o], e[o]);
+        float rl = __fsub_rn(e[o], __fsub_rn(rh, s[o]));
+        float ih = __fadd_rn(s[o + 1], e[o + 1]);
+        float il = __fsub_rn(e[o + 1], __fsub_rn(ih, s[o + 1]));
+        sm[sw(pm | s_tpos[16 * h + a])] = make_float4(__fmul_rn(rh, osc), __fmul_rn(rl, osc), __fmul_rn(ih, osc),
+                                                      __fmul_rn(il, osc));
+    }
+}
+
+}  // namespace tc

@@ -12,6 +12,7 @@
 #include <cstring>
 #include "bs_internal.h"
 #include "bs_ff.cuh"
+#include "bs_tc.cuh"
 
 namespace {
 
@@ -21,10 +22,13 @@ __device__ __forceinline__ int insert0(int x, int bit) {
     int low = x & ((1 << bit) - 1);
     return ((x >> bit) << (bit + 1)) | low;
 }
+// shared-memory index of tile element j: swizzled (tensor-core sweep) or plain
+template <bool SW>
+__device__ __forceinline__ int sx(int j) { return SW ? tc::sw(j) : j; }
 __device__ __forceinline__ cff f4c(float4 v) { return {v.x, v.y, v.z, v.w}; }
 __device__ __forceinline__ float4 c4f(const cff& c) { return make_float4(c.rh, c.rl, c.ih, c.il); }
 
-template <int K>
+template <int K, bool SW = false>
 __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* __restrict__ mats) {
     constexpr int D = 1 << K;
     int pos[K];
@@ -50,15 +54,16 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
         for (int gr = threadIdx.x; gr < ngroups; gr += blockDim.x) {
             const int jb = insert0(gr, pos[0]);
             if ((jb & (int)lcm) != (int)lcv) continue;
-            const cff a = f4c(sm[jb]), b = f4c(sm[jb | b0]);
+            const int ia = sx<SW>(jb), ib = sx<SW>(jb | b0);
+            const cff a = f4c(sm[ia]), b = f4c(sm[ib]);
             ffacc ar, ai;
             cmac_first(ar, ai, m00, a);
             cmac(ar, ai, m01, b);
             const cff ya = cdone(ar, ai);
             cmac_first(ar, ai, m10, a);
             cmac(ar, ai, m11, b);
-            sm[jb | b0] = c4f(cdone(ar, ai));
-            sm[jb] = c4f(ya);
+            sm[ib] = c4f(cdone(ar, ai));
+            sm[ia] = c4f(ya);
         }
         return;
     }
@@ -74,8 +79,8 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
             int j = jb;
 #pragma unroll
             for (int q = 0; q < K; q++) if ((c >> q) & 1) j |= 1 << tb[q];
-            idx[c] = j;
-            x[c] = f4c(sm[j]);
+            idx[c] = sx<SW>(j);
+            x[c] = f4c(sm[idx[c]]);
         }
 #pragma unroll
         for (int r = 0; r < D; r++) {
@@ -89,7 +94,7 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
 }
 
 // monomial gate: column c goes to row perm[2c] with phase i^perm[2c+1]
-template <int K>
+template <int K, bool SW = false>
 __device__ void tile_monomial(float4* sm, int T, const TileGate& g, const int32_t* __restrict__ perms) {
     constexpr int D = 1 << K;
     int pos[K];
@@ -114,8 +119,8 @@ __device__ void tile_monomial(float4* sm, int T, const TileGate& g, const int32_
             int j = jb;
 #pragma unroll
             for (int q = 0; q < K; q++) if ((c >> q) & 1) j |= 1 << g.tbit[q];
-            idx[c] = j;
-            x[c] = sm[j];
+            idx[c] = sx<SW>(j);
+            x[c] = sm[idx[c]];
         }
 #pragma unroll
         for (int c = 0; c < D; c++) {
@@ -133,23 +138,26 @@ __device__ __forceinline__ bool parity_odd(const TileGate& g, int64_t gi) {
     return par & 1;
 }
 
+// off_tab[h] << osh: global offset of the tile's high-bit pattern h
+template <typename OT, bool SW = false>
 __device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const float4* __restrict__ mats,
-                          int64_t base, const int64_t* off_tab) {
+                          int64_t base, const OT* off_tab, int osh) {
     const int nt = 1 << T, lowmask = (1 << L) - 1;
     const float4* m = mats + g.mat_off;
     for (int j = threadIdx.x; j < nt; j += blockDim.x) {
         if ((j & (int)g.lc_mask) != (int)g.lc_val) continue;
-        int64_t gi = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+        int64_t gi = base | ((int64_t)off_tab[j >> L] << osh) | (int64_t)(j & lowmask);
+        const int js = sx<SW>(j);
         int di = 0;
         for (int q = 0; q < g.k; q++) di |= (int)((gi >> g.gbit[q]) & 1) << q;
         float4 d = __ldg(m + di);
         if (d.y == 0.f && d.w == 0.f) {
             if (d.z == 0.f && d.x == 1.f) continue;
-            if (d.z == 0.f && d.x == -1.f) { sm[j] = c4f(cmul_ipow(f4c(sm[j]), 2)); continue; }
-            if (d.x == 0.f && d.z == 1.f) { sm[j] = c4f(cmul_ipow(f4c(sm[j]), 1)); continue; }
-            if (d.x == 0.f && d.z == -1.f) { sm[j] = c4f(cmul_ipow(f4c(sm[j]), 3)); continue; }
+            if (d.z == 0.f && d.x == -1.f) { sm[js] = c4f(cmul_ipow(f4c(sm[js]), 2)); continue; }
+            if (d.x == 0.f && d.z == 1.f) { sm[js] = c4f(cmul_ipow(f4c(sm[js]), 1)); continue; }
+            if (d.x == 0.f && d.z == -1.f) { sm[js] = c4f(cmul_ipow(f4c(sm[js]), 3)); continue; }
         }
-        sm[j] = c4f(cmul(f4c(d), f4c(sm[j])));
+        sm[js] = c4f(cmul(f4c(d), f4c(sm[js])));
     }
 }
 
@@ -193,7 +201,7 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
                 if (parity_odd(g, gi)) { float4 v = smem[j]; smem[j] = make_float4(-v.x, -v.y, -v.z, -v.w); }
             }
         } else if (kind == 1) {
-            tile_diag(smem, T, L, g, d.mats, base, off_tab);
+            tile_diag(smem, T, L, g, d.mats, base, off_tab, 0);
         } else if (kind == 0) {
             if (k == 1) tile_dense<1>(smem, T, g, d.mats);
             else if (k == 2 || KMAX == 2) tile_dense<2>(smem, T, g, d.mats);
@@ -210,6 +218,107 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
     for (int j = threadIdx.x; j < nt; j += blockDim.x) {
         int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
         __stcs(psi + gidx, store_c128(f4c(smem[j])));
+    }
+}
+
+// Sweep with fused 5-bit unitaries on the tensor cores (gate kind 4), T = 12, L = 5.
+// Dynamic shared memory: 48 KiB matrix digit slices | 64 KiB tile | 512 B offset table, so that
+// two CTAs fit on an SM; each holds 256 of the SM's 512 TMEM columns (from its first to its last
+// fused gate), so one CTA's MMAs overlap the other's CUDA-core work.  The tile is stored with the
+// bank swizzle tc::sw.
+constexpr int kTcSmem = 49152 + 65536 + 512;
+
+__global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ psi, SweepDesc d, int64_t tile0,
+                                                          int tc_last) {
+    extern __shared__ __align__(16) unsigned char dsm[];   // no-swizzle operands need 16-byte alignment
+    uint16_t* sB = reinterpret_cast<uint16_t*>(dsm);
+    float4* smem = reinterpret_cast<float4*>(dsm + 49152);
+    uint32_t* off32 = reinterpret_cast<uint32_t*>(dsm + 49152 + 65536);   // global offset >> 5 per high pattern
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ uint32_t s_tmem;
+    __shared__ int64_t s_base;
+    __shared__ int s_fail;
+    __shared__ int s_tpos[32];
+    __shared__ uint8_t s_emax[256];
+    constexpr int T = 12, L = 5, H = 7, nt = 1 << T, lowmask = (1 << L) - 1;
+    const int64_t tile = tile0 + (int64_t)blockIdx.x;
+    if (threadIdx.x == 0) {
+        int64_t base = 0;
+        int src = 0;
+        for (int bit = 0; bit < d.n_bits; bit++)
+            if (!((d.tile_mask >> bit) & 1ULL)) { base |= ((tile >> src) & 1LL) << bit; src++; }
+        s_base = base;
+        s_fail = 0;
+        tc::mbar_init(tc::su32(&bars[0]));
+        tc::mbar_init(tc::su32(&bars[1]));
+    }
+    for (int i = threadIdx.x; i < (1 << H); i += blockDim.x) {
+        int64_t o = 0;
+        for (int j = 0; j < H; j++) if ((i >> j) & 1) o |= 1LL << d.hi_bits[j];
+        off32[i] = (uint32_t)(o >> L);
+    }
+    __syncthreads();
+    const int64_t base = s_base;
+    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        const int64_t gidx = base | ((int64_t)off32[j >> L] << L) | (int64_t)(j & lowmask);
+        smem[tc::sw(j)] = c4f(load_c128(__ldcs(psi + gidx)));
+    }
+    __syncthreads();
+    tc::State st{0u, tc::su32(&bars[0]), tc::su32(&bars[1]), 0u, 0u};
+    bool have = false;
+    const int warp = threadIdx.x >> 5;
+    for (int gi = 0; gi < d.n_gates; gi++) {
+        const TileGate& g = d.gates[gi];
+        if ((base & (int64_t)g.gc_mask) != (int64_t)g.gc_val) continue;
+        const int kind = g.kind, k = g.k;
+        if (kind == 4) {
+            if (s_fail) continue;
+            if (!have) {
+                if (warp == 0) tc::tmem_alloc(tc::su32(&s_tmem));
+                tc::fence_before();
+                __syncthreads();
+                tc::fence_after();
+                st.tmem = s_tmem;
+                have = true;
+            }
+            tc::apply(smem, g, d.tc_pool, sB, st, base, s_emax, s_tpos, &s_fail, d.err);
+            if (gi == tc_last) {
+                __syncthreads();
+                if (warp == 0) tc::tmem_dealloc(st.tmem);
+                have = false;
+            }
+        } else if (kind == 3) {
+            for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+                const int64_t gg = base | ((int64_t)off32[j >> L] << L) | (int64_t)(j & lowmask);
+                if (parity_odd(g, gg)) {
+                    const int js = tc::sw(j);
+                    float4 v = smem[js];
+                    smem[js] = make_float4(-v.x, -v.y, -v.z, -v.w);
+                }
+            }
+        } else if (kind == 1) {
+            tile_diag<uint32_t, true>(smem, T, L, g, d.mats, base, off32, L);
+        } else if (kind == 0) {   // the planner routes sweeps with unfused 3- or 4-target gates elsewhere
+            if (k == 1) tile_dense<1, true>(smem, T, g, d.mats);
+            else tile_dense<2, true>(smem, T, g, d.mats);
+        } else {
+            if (k == 1) tile_monomial<1, true>(smem, T, g, d.perms);
+            else tile_monomial<2, true>(smem, T, g, d.perms);
+        }
+        __syncthreads();
+    }
+    if (have) {
+        // a wait gave up: give the copies and MMAs in flight a bounded time to land before releasing TMEM
+        if (threadIdx.x == 0 && s_fail) {
+            tc::mbar_wait(st.bar_u, st.ph_u);
+            tc::mbar_wait(st.bar_m, st.ph_m);
+        }
+        __syncthreads();
+        if (warp == 0) tc::tmem_dealloc(st.tmem);
+    }
+    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        const int64_t gidx = base | ((int64_t)off32[j >> L] << L) | (int64_t)(j & lowmask);
+        __stcs(psi + gidx, store_c128(f4c(smem[tc::sw(j)])));
     }
 }
 
@@ -704,9 +813,17 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     std::vector<TileGate> tg;
     std::vector<float4> mats;
     std::vector<int32_t> perms;
-    struct Launch { int64_t gate0; int n_gates; std::vector<int> hi; bool big; int big_gate; int kmax = 1; };
+    struct Launch {
+        int64_t gate0; int n_gates; std::vector<int> hi; bool big; int big_gate; int kmax = 1;
+        int tc_last = -1;          // index (within the sweep) of the last fused tensor-core gate, -1 if none
+        int n_tc = 0;
+    };
     std::vector<Launch> launches;
     std::vector<int32_t> big_bits;
+    std::vector<uint16_t> tc_pool;
+    const bool c64 = s->precision == BS_PREC_C64;
+    const bool use_tc = bs_tc_enabled() && !c64 && T == 12 && L == 5;
+    std::vector<HostGate> fused;
     for (const Sweep& sw : sweeps) {
         Launch ln;
         ln.gate0 = (int64_t)tg.size();
@@ -719,7 +836,37 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         for (int b = 0; b < 64; b++) local[b] = -1;
         for (int b = 0; b < L; b++) local[b] = b;
         for (size_t i = 0; i < sw.hi_bits.size(); i++) local[sw.hi_bits[i]] = L + (int)i;
-        for (const HostGate& hg : sw.gates) {
+        const std::vector<HostGate>* glist = &sw.gates;
+        if (use_tc && (int)sw.hi_bits.size() == T - L) {
+            bs_fuse_tc(sw.gates, local, T, fused);
+            // the tensor-core sweep kernel carries float-float paths for 1- and 2-target gates only
+            bool ok = true;
+            for (const HostGate& hg : fused) if (hg.kind != 1 && hg.kind != 4 && hg.k >= 3) ok = false;
+            if (ok) glist = &fused;
+        }
+        for (const HostGate& hg : *glist) {
+            if (hg.kind == 4) {
+                TileGate t{};
+                t.kind = 4;
+                t.k = 5;
+                for (int q = 0; q < 5; q++) t.gbit[q] = local[hg.ebit[q]];
+                const int nvar = 1 << hg.ubits.size();
+                t.tc_nu = (int32_t)hg.ubits.size();
+                for (size_t i = 0; i < hg.ubits.size(); i++) t.tc_ub[i] = hg.ubits[i];
+                t.tc_off = (int32_t)(tc_pool.size() / tc::kPoolBlock);
+                tc_pool.resize(tc_pool.size() + (size_t)nvar * tc::kPoolBlock);
+                int eu = 0;
+                bool ok = bs_tc_exponent(hg.mat.data(), nvar, eu);
+                for (int v = 0; v < nvar && ok; v++)
+                    ok = bs_tc_digits(hg.mat.data() + (size_t)v * 2048, tc_pool.data() + (size_t)(t.tc_off + v) * tc::kPoolBlock, eu);
+                if (!ok) return bs_fail(s, BS_ERR_INVALID_ARG, "fused gate matrix out of range");
+                t.tc_eu = eu;
+                ln.tc_last = ln.n_gates;
+                ln.n_tc++;
+                tg.push_back(t);
+                ln.n_gates++;
+                continue;
+            }
             // consecutive CZ gates (Z on one bit, one control at value 1) merge into one parity-phase gate
             if (hg.kind == 1 && hg.k == 1 && hg.mat.size() == 4 && hg.mat[0] == 1.0 && hg.mat[1] == 0.0 &&
                 hg.mat[2] == -1.0 && hg.mat[3] == 0.0 && __builtin_popcountll(hg.cmask) == 1 && hg.cval == hg.cmask) {
@@ -816,7 +963,7 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     std::vector<RBSeg> segs;
     std::vector<int64_t> seg0(launches.size(), -1), nseg(launches.size(), 0);
     for (size_t li = 0; li < launches.size() && !rb_off; li++) {
-        if (launches[li].big) continue;
+        if (launches[li].big || launches[li].tc_last >= 0) continue;
         std::vector<RBSeg> ss = rb_segments(tg, launches[li].gate0, launches[li].n_gates, T);
         if (ss.empty()) continue;
         seg0[li] = (int64_t)segs.size();
@@ -829,9 +976,12 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     int64_t b_m = al((int64_t)mats.size() * (int64_t)sizeof(float4));
     int64_t b_p = al((int64_t)(perms.size() + big_bits.size() + 1) * (int64_t)sizeof(int32_t));
     int64_t b_s = al((int64_t)(segs.size() + 1) * (int64_t)sizeof(RBSeg));
-    int rc = bs_ensure_plan(s, b_tg + b_m + b_p + b_s);
+    int64_t b_tc = al((int64_t)tc_pool.size() * (int64_t)sizeof(uint16_t));
+    int rc = bs_ensure_plan(s, b_tg + b_m + b_p + b_s + b_tc);
     if (rc) return rc;
-    std::vector<char> host((size_t)(b_tg + b_m + b_p + b_s), 0);
+    std::vector<char> host((size_t)(b_tg + b_m + b_p + b_s + b_tc), 0);
+    if (!tc_pool.empty())
+        std::memcpy(host.data() + b_tg + b_m + b_p + b_s, tc_pool.data(), tc_pool.size() * sizeof(uint16_t));
     if (!segs.empty()) std::memcpy(host.data() + b_tg + b_m + b_p, segs.data(), segs.size() * sizeof(RBSeg));
     if (!tg.empty()) std::memcpy(host.data(), tg.data(), tg.size() * sizeof(TileGate));
     if (!mats.empty()) std::memcpy(host.data() + b_tg, mats.data(), mats.size() * sizeof(float4));
@@ -867,10 +1017,23 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         cudaFuncSetAttribute(k_tile_rb<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
         cudaFuncSetAttribute(k_tile_rb<1>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         cudaFuncSetAttribute(k_tile_rb<2>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+        cudaFuncSetAttribute(k_tile_sweep_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+        cudaFuncSetAttribute(k_tile_sweep_tc, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         attr_set[s->device & 63] = true;
     }
     double2* psi = (double2*)s->state;
-    const bool c64 = s->precision == BS_PREC_C64;
+    const uint16_t* d_tc = (const uint16_t*)(dev + b_tg + b_m + b_p + b_s);
+    if (!tc_pool.empty()) {
+        if (!s->dev_flag) {
+            rc = bs_cuda_check(s, cudaMalloc((void**)&s->dev_flag, 256), "flag alloc");
+            if (rc) return rc;
+        }
+        if (!s->flag_armed) {
+            rc = bs_cuda_check(s, cudaMemsetAsync(s->dev_flag, 0, sizeof(int), s->stream), "flag reset");
+            if (rc) return rc;
+            s->flag_armed = true;
+        }
+    }
     const double esz = c64 ? 8.0 : 16.0;          // bytes per stored amplitude
     const int64_t ntiles = (int64_t)1 << (n_bits - T);
     const RBSeg* d_seg = (const RBSeg*)(dev + b_tg + b_m + b_p);
@@ -908,9 +1071,13 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         d.gates = d_tg + ln.gate0;
         d.mats = d_m;
         d.perms = d_p;
+        d.tc_pool = d_tc;
+        d.err = s->dev_flag;
         for (int64_t t0 = 0; t0 < ntiles; t0 += (1LL << 30)) {
             int64_t nb = std::min<int64_t>(ntiles - t0, 1LL << 30);
-            if (c64) {
+            if (ln.tc_last >= 0) {
+                k_tile_sweep_tc<<<(unsigned)nb, 256, kTcSmem, s->stream>>>(psi, d, t0, ln.tc_last);
+            } else if (c64) {
                 const size_t sm64 = ((size_t)1 << T) * sizeof(float2) + ((size_t)1 << H) * sizeof(int64_t);
                 if (ln.kmax <= 2) k_tile_sweep_c64<2><<<(unsigned)nb, kThreads, sm64, s->stream>>>((float2*)s->state, d, t0);
                 else k_tile_sweep_c64<4><<<(unsigned)nb, kThreads, sm64, s->stream>>>((float2*)s->state, d, t0);
@@ -929,7 +1096,20 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         s->stats.kernel_launches++;
         s->stats.sweeps++;
         s->stats.gates += ln.n_gates;
+        s->stats.tc_gates += ln.n_tc;
         s->stats.bytes_moved += 2.0 * esz * (double)s->len;
     }
     return bs_cuda_check(s, cudaGetLastError(), "tile sweep launch");
+}
+
+int bs_check_device_flag(bs_sim* s) {
+    if (!s->flag_armed) return BS_OK;
+    s->flag_armed = false;
+    int flag = 0;
+    int rc = bs_cuda_check(s, cudaMemcpyAsync(&flag, s->dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
+                           "flag read");
+    if (!rc) rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "flag read");
+    if (rc) return rc;
+    if (flag) return bs_fail(s, BS_ERR_TIMEOUT, "a tensor-core sweep gave up waiting for its copies or MMAs");
+    return BS_OK;
 }

@@ -79,6 +79,7 @@ typedef struct bs_stats {
     int64_t gates;             /* gates applied */
     double  bytes_moved;       /* algorithmic HBM bytes of the executed sweeps */
     double  gpu_ms;            /* device time of the call (CUDA events) */
+    int64_t tc_gates;          /* fused unitaries applied on the tensor cores (each replacing a run of gates) */
 } bs_stats;
 
 /* ---- lifecycle: StateVectorSimulator(T, n, shots) / DensityMatrixSimulator(T, n, shots)
