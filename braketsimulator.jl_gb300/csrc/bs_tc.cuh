@@ -80,6 +80,22 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
                  : "memory");
 }
 
+__device__ __forceinline__ void mbar_init_n(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void bulk_s2g(void* dst, uint32_t src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// generic-proxy shared-memory writes become visible to the async proxy (bulk copies, MMA operands)
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 __device__ __forceinline__ void tmem_alloc(uint32_t slot) {   // whole warp
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(kCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -95,6 +111,11 @@ __device__ __forceinline__ void wait_ld() { asm volatile("tcgen05.wait::ld.sync.
 __device__ __forceinline__ void st8(uint32_t taddr, const uint32_t (&w)[8]) {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(w[0]),
                  "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7])
+                 : "memory");
+}
+__device__ __forceinline__ void st4(uint32_t taddr, const uint32_t (&w)[4]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "r"(w[0]), "r"(w[1]),
+                 "r"(w[2]), "r"(w[3])
                  : "memory");
 }
 __device__ __forceinline__ void ld8(uint32_t taddr, uint32_t (&r)[8]) {
@@ -142,10 +163,11 @@ __device__ __forceinline__ float two_sum(float& s, float g) {
 }
 
 struct State {
-    uint32_t tmem;       // TMEM base address
-    uint32_t bar_u;      // digit-slice copy completion
-    uint32_t bar_m;      // MMA completion
-    uint32_t ph_u, ph_m; // expected phase parities
+    uint32_t tmem;             // TMEM base address
+    uint32_t bar_u;            // digit-slice copy completion (1 arrival + bytes)
+    uint32_t bar_m;            // MMA completion (commit)
+    uint32_t bar_r;            // accumulator read by every warp (8 arrivals)
+    uint32_t ph_u, ph_m, ph_r; // expected phase parities
 };
 
 // Thread 0: issue the MMAs of one digit-weight round into D, then commit to bar_m.
@@ -171,7 +193,7 @@ __device__ __forceinline__ void issue_round(const State& st, uint32_t bB, int ro
 // On a wait that gives up, sets *fail and *err and leaves the tile partly updated.
 __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint16_t* __restrict__ pool, uint16_t* sB,
                                       State& st, int64_t base, uint8_t* s_emax, int* s_tpos, int* s_fail, int* err) {
-    const int tid = threadIdx.x, warp = tid >> 5, m = tid & 127, h = tid >> 7;
+    const int tid = threadIdx.x, warp = tid >> 5, lane_id = tid & 31, m = tid & 127, h = tid >> 7;
     if (tid == 0) {
         // the previous readers of sB (the MMAs of the previous fused gate) have completed
         int var = 0;
@@ -198,9 +220,9 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
     uint32_t eb = 0;
 #pragma unroll 4
     for (int a = 0; a < 16; a++) {
-        const float4 v = sm[sw(pm | s_tpos[16 * h + a])];
-        eb = max(eb, (__float_as_uint(v.x) >> 23) & 0xFFu);
-        eb = max(eb, (__float_as_uint(v.z) >> 23) & 0xFFu);
+        const float4 va = sm[sw(pm | s_tpos[16 * h + a])];
+        eb = max(eb, (__float_as_uint(va.x) >> 23) & 0xFFu);
+        eb = max(eb, (__float_as_uint(va.z) >> 23) & 0xFFu);
     }
     s_emax[tid] = (uint8_t)eb;
     __syncthreads();
@@ -209,20 +231,20 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
     const float sc = __uint_as_float((uint32_t)(260 - ebc) << 23);                 // 2^(7 - E)
     const float osc = __uint_as_float((uint32_t)(ebc - 13 + g.tc_eu) << 23);       // 2^(E + eu - 14)
     const uint32_t lane = (uint32_t)((warp & 3) * 32) << 16;
-#pragma unroll 1
-    for (int c = 0; c < 2; c++) {
-        uint32_t w[6][8];
 #pragma unroll
-        for (int a = 0; a < 8; a++) {
-            const float4 v = sm[sw(pm | s_tpos[16 * h + 8 * c + a])];
+    for (int c = 0; c < 4; c++) {
+        uint32_t w[6][4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            const float4 vv = sm[sw(pm | s_tpos[16 * h + 4 * c + a])];
             float qr[6], qi[6];
-            digits(__fmul_rn(v.x, sc), __fmul_rn(v.y, sc), qr);
-            digits(__fmul_rn(v.z, sc), __fmul_rn(v.w, sc), qi);
+            digits(__fmul_rn(vv.x, sc), __fmul_rn(vv.y, sc), qr);
+            digits(__fmul_rn(vv.z, sc), __fmul_rn(vv.w, sc), qi);
 #pragma unroll
             for (int j = 0; j < 6; j++) w[j][a] = __byte_perm(__float_as_uint(qr[j]), __float_as_uint(qi[j]), 0x7632);
         }
 #pragma unroll
-        for (int j = 0; j < 6; j++) st8(st.tmem + lane + (uint32_t)(kA0 + 32 * j + 16 * h + 8 * c), w[j]);
+        for (int j = 0; j < 6; j++) st4(st.tmem + lane + (uint32_t)(kA0 + 32 * j + 16 * h + 4 * c), w[j]);
     }
     wait_st();
     fence_before();
@@ -234,16 +256,20 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
         else { *s_fail = 1; atomicExch(err, 1); }
     }
     st.ph_u ^= 1u;
-    // running float-float sums of the thread's 32 outputs (16 amplitudes x re/im)
+    __syncthreads();
+    if (*s_fail) return;
+    // Five rounds.  Every warp waits for the round's MMAs itself, folds the accumulator into its
+    // running float-float sums (the thread's 16 amplitudes x re/im) and arrives on bar_r; thread 0
+    // starts the next round once all eight warps have read the accumulator.
     float s[32], e[32];
+    bool ok = true;
 #pragma unroll 1
     for (int round = 0; round < 5; round++) {
-        if (tid == 0 && !*s_fail) {
-            if (!mbar_wait(st.bar_m, st.ph_m)) { *s_fail = 1; atomicExch(err, 1); }
-        }
+        uint32_t done = 1;
+        if (lane_id == 0) done = mbar_wait(st.bar_m, st.ph_m) ? 1u : 0u;
+        done = __shfl_sync(0xffffffffu, done, 0);
         st.ph_m ^= 1u;
-        __syncthreads();
-        if (*s_fail) return;
+        if (!done) { ok = false; break; }
         fence_after();
 #pragma unroll
         for (int c = 0; c < 4; c++) {
@@ -260,10 +286,23 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
             }
         }
         fence_before();
-        __syncthreads();
-        fence_after();
-        // D is free again: start the next round (the other CTA on the SM runs meanwhile)
-        if (round < 4 && tid == 0) issue_round(st, bB, round + 1);
+        __syncwarp();
+        if (lane_id == 0) mbar_arrive(st.bar_r);
+        if (round < 4 && tid == 0) {
+            if (mbar_wait(st.bar_r, st.ph_r)) {
+                fence_after();
+                issue_round(st, bB, round + 1);
+            } else {
+                ok = false;
+            }
+        }
+        st.ph_r ^= 1u;
+        if (!ok) break;
+    }
+    if (!ok) {
+        *s_fail = 1;
+        atomicExch(err, 1);
+        return;
     }
 #pragma unroll
     for (int a = 0; a < 16; a++) {

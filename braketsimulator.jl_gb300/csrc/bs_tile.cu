@@ -230,11 +230,12 @@ constexpr int kTcSmem = 49152 + 65536 + 512;
 
 __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ psi, SweepDesc d, int64_t tile0,
                                                           int tc_last) {
-    extern __shared__ __align__(16) unsigned char dsm[];   // no-swizzle operands need 16-byte alignment
+    // 128-byte alignment: each 128-byte core matrix of the matrix operand sits in one shared-memory line
+    extern __shared__ __align__(128) unsigned char dsm[];
     uint16_t* sB = reinterpret_cast<uint16_t*>(dsm);
     float4* smem = reinterpret_cast<float4*>(dsm + 49152);
     uint32_t* off32 = reinterpret_cast<uint32_t*>(dsm + 49152 + 65536);   // global offset >> 5 per high pattern
-    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ __align__(8) uint64_t bars[3];   // digit copy, MMA, accumulator read
     __shared__ uint32_t s_tmem;
     __shared__ int64_t s_base;
     __shared__ int s_fail;
@@ -251,6 +252,7 @@ __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ 
         s_fail = 0;
         tc::mbar_init(tc::su32(&bars[0]));
         tc::mbar_init(tc::su32(&bars[1]));
+        tc::mbar_init_n(tc::su32(&bars[2]), 8);
     }
     for (int i = threadIdx.x; i < (1 << H); i += blockDim.x) {
         int64_t o = 0;
@@ -259,14 +261,22 @@ __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ 
     }
     __syncthreads();
     const int64_t base = s_base;
-    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
-        const int64_t gidx = base | ((int64_t)off32[j >> L] << L) | (int64_t)(j & lowmask);
-        smem[tc::sw(j)] = c4f(load_c128(__ldcs(psi + gidx)));
+    const int warp = threadIdx.x >> 5;
+    // tile load: each thread's 16 loads are issued together (coalesced 512 B rows), then converted to
+    // float-float at the swizzled positions
+    {
+        double2 x[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const int j = i * 256 + (int)threadIdx.x;
+            x[i] = __ldcs(psi + (base | ((int64_t)off32[j >> L] << L) | (int64_t)(j & lowmask)));
+        }
+#pragma unroll
+        for (int i = 0; i < 16; i++) smem[tc::sw(i * 256 + (int)threadIdx.x)] = c4f(load_c128(x[i]));
     }
     __syncthreads();
-    tc::State st{0u, tc::su32(&bars[0]), tc::su32(&bars[1]), 0u, 0u};
+    tc::State st{0u, tc::su32(&bars[0]), tc::su32(&bars[1]), tc::su32(&bars[2]), 0u, 0u, 0u};
     bool have = false;
-    const int warp = threadIdx.x >> 5;
     for (int gi = 0; gi < d.n_gates; gi++) {
         const TileGate& g = d.gates[gi];
         if ((base & (int64_t)g.gc_mask) != (int64_t)g.gc_val) continue;
@@ -316,9 +326,11 @@ __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ 
         __syncthreads();
         if (warp == 0) tc::tmem_dealloc(st.tmem);
     }
-    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
-        const int64_t gidx = base | ((int64_t)off32[j >> L] << L) | (int64_t)(j & lowmask);
-        __stcs(psi + gidx, store_c128(f4c(smem[tc::sw(j)])));
+    // tile store: streaming stores, nothing waits for them
+#pragma unroll 4
+    for (int i = 0; i < 16; i++) {
+        const int j = i * 256 + (int)threadIdx.x;
+        __stcs(psi + (base | ((int64_t)off32[j >> L] << L) | (int64_t)(j & lowmask)), store_c128(f4c(smem[tc::sw(j)])));
     }
 }
 
