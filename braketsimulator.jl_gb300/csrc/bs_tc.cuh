@@ -55,15 +55,17 @@ __device__ __forceinline__ void mbar_init(uint32_t bar) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// bounded wait for the phase with the given parity; false if it did not complete in kSpin cycles
+// bounded wait for the phase with the given parity; false if it did not complete in kSpin cycles.
+// Each try_wait suspends the thread until the phase completes or ~20 us pass, so waiting warps do not
+// take issue slots from the working ones.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     const long long t0 = clock64();
     while (true) {
         uint32_t done;
         asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
-            : "r"(bar), "r"(parity)
+            : "r"(bar), "r"(parity), "r"(20000u)
             : "memory");
         if (done) return true;
         if (clock64() - t0 > kSpin) return false;

@@ -834,7 +834,11 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     std::vector<int32_t> big_bits;
     std::vector<uint16_t> tc_pool;
     const bool c64 = s->precision == BS_PREC_C64;
-    const bool use_tc = bs_tc_enabled() && !c64 && T == 12 && L == 5;
+    // measured on GB300: fused tensor-core sweeps win from 27 vector bits up and lose below
+    // (per-CTA overheads over too few tiles); BS_TC_MIN_BITS overrides the threshold
+    const char* tmb = getenv("BS_TC_MIN_BITS");
+    const int tc_min_bits = tmb ? atoi(tmb) : 27;
+    const bool use_tc = bs_tc_enabled() && !c64 && T == 12 && L == 5 && n_bits >= tc_min_bits;
     std::vector<HostGate> fused;
     for (const Sweep& sw : sweeps) {
         Launch ln;

@@ -15,20 +15,24 @@ TOL = 1e-12
 
 
 class tc_mode:
-    """BS_TC=0 keeps every gate on the float-float tile path; it is read on every evolve."""
+    """BS_TC=0 keeps every gate on the float-float tile path; BS_TC_MIN_BITS lowers the state size
+    from which fused tensor-core sweeps are used (27 vector bits by default) so that oracle-sized
+    cases exercise them.  Both are read on every evolve."""
 
     def __init__(self, on):
         self.on = on
 
     def __enter__(self):
-        self.old = os.environ.get("BS_TC")
+        self.old = {k: os.environ.get(k) for k in ("BS_TC", "BS_TC_MIN_BITS")}
         os.environ["BS_TC"] = "1" if self.on else "0"
+        os.environ["BS_TC_MIN_BITS"] = "12"
 
     def __exit__(self, *a):
-        if self.old is None:
-            os.environ.pop("BS_TC", None)
-        else:
-            os.environ["BS_TC"] = self.old
+        for k, v in self.old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
 
 
 def haar(rng, d=2):
