@@ -55,6 +55,8 @@ class BsStats(C.Structure):
         ("bytes_moved", C.c_double),
         ("gpu_ms", C.c_double),
         ("tc_gates", C.c_int64),
+        ("tc_launches", C.c_int64),
+        ("tc_ms", C.c_double),
     ]
 
 

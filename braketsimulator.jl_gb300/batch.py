@@ -50,5 +50,6 @@ def batch_simulate(circuits, qubit_counts, observables=(), shots: int = 0, seed:
         raise _abi.BraketGB300Error(rc, "bs_run_batch failed")
     del keeps
     stats = {"sweeps": st.sweeps, "kernel_launches": st.kernel_launches, "gates": st.gates,
-             "bytes_moved": st.bytes_moved, "gpu_ms": st.gpu_ms, "tc_gates": st.tc_gates}
+             "bytes_moved": st.bytes_moved, "gpu_ms": st.gpu_ms, "tc_gates": st.tc_gates,
+                "tc_launches": st.tc_launches, "tc_ms": st.tc_ms}
     return exp[: nc * n_terms].reshape(nc, n_terms), smp[: nc * shots].reshape(nc, shots), stats

@@ -32,20 +32,23 @@ __device__ __forceinline__ cff f4c(float4 v) { return {v.x, v.y, v.z, v.w}; }
 __device__ __forceinline__ float4 c4f(const cff& c) { return make_float4(c.rh, c.rl, c.ih, c.il); }
 
 // lambda_i = sum_t c_t (-i)^ph_t (-1)^popc(i & zm_t) psi_{i ^ xm_t}
-__global__ void __launch_bounds__(kAThreads) k_pauli_sum(const double2* __restrict__ psi, double2* __restrict__ lam,
-                                                         int64_t n, const PauliTerm* __restrict__ terms, int nt) {
+// C64: complex64 storage; the arithmetic and the sums stay float-float either way.
+template <bool C64>
+__global__ void __launch_bounds__(kAThreads) k_pauli_sum(const typename Elem<C64>::T* __restrict__ psi,
+                                                         typename Elem<C64>::T* __restrict__ lam, int64_t n,
+                                                         const PauliTerm* __restrict__ terms, int nt) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         ffacc ar{0.f, 0.f}, ai{0.f, 0.f};
         for (int t = 0; t < nt; t++) {
             PauliTerm p = terms[t];
-            cff x = load_c128(psi[i ^ (int64_t)p.xm]);
+            cff x = Elem<C64>::load(psi[i ^ (int64_t)p.xm]);
             int ph = p.ph + ((__popcll((unsigned long long)i & p.zm) & 1) ? 2 : 0);
             // (-i)^ph: multiply x by i^(4-ph)
             x = cmul_ipow(x, (4 - (ph & 3)) & 3);
             acc_add(ar, p.ch, p.cl, x.rh, x.rl);
             acc_add(ai, p.ch, p.cl, x.ih, x.il);
         }
-        lam[i] = store_c128(cdone(ar, ai));
+        lam[i] = Elem<C64>::store(cdone(ar, ai));
     }
 }
 
@@ -71,11 +74,13 @@ __device__ void block_sum2(double a, double b, double* out2) {
 }
 
 // <a|b> (complex) into out2[0..1]
-__global__ void __launch_bounds__(kAThreads) k_inner(const double2* __restrict__ a, const double2* __restrict__ b,
-                                                     int64_t n, double* __restrict__ out2) {
+template <bool C64>
+__global__ void __launch_bounds__(kAThreads) k_inner(const typename Elem<C64>::T* __restrict__ a,
+                                                     const typename Elem<C64>::T* __restrict__ b, int64_t n,
+                                                     double* __restrict__ out2) {
     ffsum sr{0.f, 0.f}, si{0.f, 0.f};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        cff x = load_c128(a[i]), y = load_c128(b[i]);
+        cff x = Elem<C64>::load(a[i]), y = Elem<C64>::load(b[i]);
         ffacc r, m;
         acc_first(r, x.rh, x.rl, y.rh, y.rl);
         acc_add(r, x.ih, x.il, y.ih, y.il);
@@ -182,8 +187,10 @@ __device__ void adj_apply(float4* sm, int T, int L, const TileGate& g, const flo
     }
 }
 
-__global__ void __launch_bounds__(kAThreads) k_adjoint_sweep(double2* __restrict__ psi, double2* __restrict__ lam,
-                                                             SweepDesc d, const AdjGate* __restrict__ ag,
+template <bool C64>
+__global__ void __launch_bounds__(kAThreads) k_adjoint_sweep(typename Elem<C64>::T* __restrict__ psi,
+                                                             typename Elem<C64>::T* __restrict__ lam, SweepDesc d,
+                                                             const AdjGate* __restrict__ ag,
                                                              double* __restrict__ grad_acc, int64_t tile0) {
     extern __shared__ float4 smem[];
     const int T = d.T, L = d.L, H = T - L;
@@ -210,8 +217,8 @@ __global__ void __launch_bounds__(kAThreads) k_adjoint_sweep(double2* __restrict
     const int lowmask = (1 << L) - 1;
     for (int j = threadIdx.x; j < nt; j += blockDim.x) {
         int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
-        sp[j] = c4f(load_c128(psi[gidx]));
-        sl[j] = c4f(load_c128(lam[gidx]));
+        sp[j] = c4f(Elem<C64>::load(psi[gidx]));
+        sl[j] = c4f(Elem<C64>::load(lam[gidx]));
     }
     __syncthreads();
     for (int gi = 0; gi < d.n_gates; gi++) {
@@ -258,8 +265,8 @@ __global__ void __launch_bounds__(kAThreads) k_adjoint_sweep(double2* __restrict
     }
     for (int j = threadIdx.x; j < nt; j += blockDim.x) {
         int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
-        psi[gidx] = store_c128(f4c(sp[j]));
-        lam[gidx] = store_c128(f4c(sl[j]));
+        psi[gidx] = Elem<C64>::store(f4c(sp[j]));
+        lam[gidx] = Elem<C64>::store(f4c(sl[j]));
     }
 }
 
@@ -311,7 +318,8 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
                                    const double* coeffs, double* energy_out, double* grad_out) {
     if (!s) return BS_ERR_INVALID_ARG;
     if (s->kind != BS_KIND_SV) return bs_fail(s, BS_ERR_UNSUPPORTED, "adjoint gradients need a state-vector simulator");
-    if (s->precision != BS_PREC_C128) return bs_fail(s, BS_ERR_UNSUPPORTED, "adjoint gradients need a complex128 state");
+    const bool c64 = s->precision == BS_PREC_C64;
+    const size_t esz = c64 ? 8 : 16;
     if (n_ops < 0 || (n_ops && (!ops || !param_index || !gen_kind || !gen_xmask || !gen_zmask)) || n_params < 0 ||
         n_terms < 1 || !xmask || !zmask || !coeffs || !energy_out || (n_params && !grad_out))
         return bs_fail(s, BS_ERR_INVALID_ARG, "bad adjoint arguments");
@@ -328,7 +336,7 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
     cudaEventRecord(s->ev0, s->stream);
     // 2. lambda = H psi
     void* lam = nullptr;
-    rc = bs_cuda_check(s, cudaMallocAsync(&lam, (size_t)len * 16, s->stream), "lambda allocation");
+    rc = bs_cuda_check(s, cudaMallocAsync(&lam, (size_t)len * esz, s->stream), "lambda allocation");
     if (rc) return rc;
     std::vector<PauliTerm> terms((size_t)n_terms);
     for (int t = 0; t < n_terms; t++) {
@@ -347,8 +355,15 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
     cudaMemcpyAsync(d_terms, terms.data(), terms.size() * sizeof(PauliTerm), cudaMemcpyHostToDevice, s->stream);
     cudaMemsetAsync(d_acc, 0, (size_t)(n_params + 2) * 8, s->stream);
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((len + kAThreads - 1) / kAThreads, 152 * 8));
-    k_pauli_sum<<<blocks, kAThreads, 0, s->stream>>>((const double2*)s->state, (double2*)lam, len, d_terms, n_terms);
-    k_inner<<<blocks, kAThreads, 0, s->stream>>>((const double2*)s->state, (const double2*)lam, len, d_acc + n_params);
+    if (c64) {
+        k_pauli_sum<true><<<blocks, kAThreads, 0, s->stream>>>((const float2*)s->state, (float2*)lam, len, d_terms, n_terms);
+        k_inner<true><<<blocks, kAThreads, 0, s->stream>>>((const float2*)s->state, (const float2*)lam, len, d_acc + n_params);
+    } else {
+        k_pauli_sum<false><<<blocks, kAThreads, 0, s->stream>>>((const double2*)s->state, (double2*)lam, len, d_terms,
+                                                                 n_terms);
+        k_inner<false><<<blocks, kAThreads, 0, s->stream>>>((const double2*)s->state, (const double2*)lam, len,
+                                                             d_acc + n_params);
+    }
     // 3. backward: reversed, daggered gate list with gradient markers before each parameterised gate
     std::vector<BwdItem> items;
     for (int64_t i = n_ops - 1; i >= 0; i--) {
@@ -514,7 +529,8 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
     const int32_t* d_p = (const int32_t*)((char*)s->plan_buf + b_ag + b_m);
     const int H = T - L;
     const size_t smem = (size_t)2 * ((size_t)1 << T) * sizeof(float4) + ((size_t)1 << H) * sizeof(int64_t);
-    cudaFuncSetAttribute(k_adjoint_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_adjoint_sweep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_adjoint_sweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     const int64_t ntiles = (int64_t)1 << (n_bits - T);
     for (size_t sw = 0; sw < sweeps_items.size(); sw++) {
         SweepDesc d{};
@@ -529,12 +545,16 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
         d.perms = d_p;
         for (int64_t t0 = 0; t0 < ntiles; t0 += (1LL << 30)) {
             int64_t nb = std::min<int64_t>(ntiles - t0, 1LL << 30);
-            k_adjoint_sweep<<<(unsigned)nb, kAThreads, smem, s->stream>>>((double2*)s->state, (double2*)lam, d,
-                                                                           d_ag + sweep_first[sw], d_acc, t0);
+            if (c64)
+                k_adjoint_sweep<true><<<(unsigned)nb, kAThreads, smem, s->stream>>>((float2*)s->state, (float2*)lam, d,
+                                                                                     d_ag + sweep_first[sw], d_acc, t0);
+            else
+                k_adjoint_sweep<false><<<(unsigned)nb, kAThreads, smem, s->stream>>>((double2*)s->state, (double2*)lam, d,
+                                                                                      d_ag + sweep_first[sw], d_acc, t0);
         }
         s->stats.kernel_launches++;
         s->stats.sweeps++;
-        s->stats.bytes_moved += 64.0 * (double)len;
+        s->stats.bytes_moved += 4.0 * (double)esz * (double)len;
     }
     std::vector<double> res((size_t)n_params + 2);
     cudaMemcpyAsync(res.data(), d_acc, res.size() * 8, cudaMemcpyDeviceToHost, s->stream);

@@ -142,6 +142,7 @@ int bs_destroy(bs_sim* s) {
     if (s->alias_ix) cudaFree(s->alias_ix);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
+    for (cudaEvent_t e : s->tc_events) cudaEventDestroy(e);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return BS_OK;
@@ -205,6 +206,7 @@ int bs_copy_state(bs_sim* dst, const bs_sim* src) {
 int bs_synchronize(bs_sim* s) {
     if (!s) return BS_ERR_INVALID_ARG;
     int rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "synchronize");
+    if (!rc) bs_collect_tc_time(s);
     return rc ? rc : bs_check_device_flag(s);
 }
 
@@ -265,6 +267,7 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     if (!s) return BS_ERR_INVALID_ARG;
     if (n_ops < 0 || (n_ops > 0 && !ops)) return bs_fail(s, BS_ERR_INVALID_ARG, "bad op list");
     s->stats = bs_stats{};
+    s->tc_events_used = 0;
     s->alias_valid = false;
     cudaEventRecord(s->ev0, s->stream);
     std::vector<HostGate> pending;
@@ -305,6 +308,7 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     float ms = 0;
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);
     s->stats.gpu_ms = ms;
+    bs_collect_tc_time(s);
     return bs_check_device_flag(s);
 }
 

@@ -328,6 +328,8 @@ extern "C" int bs_run_batch(int n_circuits, const int* n_qubits, const bs_op* co
                 wst[(size_t)w].gates += h->stats.gates;
                 wst[(size_t)w].bytes_moved += h->stats.bytes_moved;
                 wst[(size_t)w].tc_gates += h->stats.tc_gates;
+                wst[(size_t)w].tc_launches += h->stats.tc_launches;
+                wst[(size_t)w].tc_ms += h->stats.tc_ms;
             }
             if (!r && n_terms)
                 r = bs_expectation_pauli(h, n_terms, xmask + (size_t)c * n_terms, zmask + (size_t)c * n_terms, nullptr,
@@ -351,6 +353,8 @@ extern "C" int bs_run_batch(int n_circuits, const int* n_qubits, const bs_op* co
         tot.gates += x.gates;
         tot.bytes_moved += x.bytes_moved;
         tot.tc_gates += x.tc_gates;
+        tot.tc_launches += x.tc_launches;
+        tot.tc_ms += x.tc_ms;
     }
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);

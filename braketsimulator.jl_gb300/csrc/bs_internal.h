@@ -90,6 +90,8 @@ struct bs_sim {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int* dev_flag = nullptr;      // device error flag of the tensor-core sweeps
     bool flag_armed = false;
+    std::vector<cudaEvent_t> tc_events;   // pool: an event pair around each tensor-core launch
+    size_t tc_events_used = 0;            // pairs recorded since the last bs_collect_tc_time
     bs_stats stats{};
     std::string err;
 };
@@ -129,6 +131,8 @@ bool bs_tc_exponent(const double* mat, int n_mat, int& eu);
 int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps);
 // BS_ERR_TIMEOUT if a tensor-core sweep since the last check gave up on a bounded wait
 int bs_check_device_flag(bs_sim* s);
+// After the stream has synchronised: add the device time of the recorded tensor-core launches to stats.tc_ms
+void bs_collect_tc_time(bs_sim* s);
 
 // ---- reference-compat Kraus (bs_dm.cu)
 int bs_kraus_reference(bs_sim* s, const double* kraus, int nk, int k, const int* targets,

@@ -1092,7 +1092,18 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         for (int64_t t0 = 0; t0 < ntiles; t0 += (1LL << 30)) {
             int64_t nb = std::min<int64_t>(ntiles - t0, 1LL << 30);
             if (ln.tc_last >= 0) {
+                const size_t pe = 2 * s->tc_events_used;
+                while (s->tc_events.size() < pe + 2) {
+                    cudaEvent_t e;
+                    rc = bs_cuda_check(s, cudaEventCreate(&e), "event");
+                    if (rc) return rc;
+                    s->tc_events.push_back(e);
+                }
+                cudaEventRecord(s->tc_events[pe], s->stream);
                 k_tile_sweep_tc<<<(unsigned)nb, 256, kTcSmem, s->stream>>>(psi, d, t0, ln.tc_last);
+                cudaEventRecord(s->tc_events[pe + 1], s->stream);
+                s->tc_events_used++;
+                s->stats.tc_launches++;
             } else if (c64) {
                 const size_t sm64 = ((size_t)1 << T) * sizeof(float2) + ((size_t)1 << H) * sizeof(int64_t);
                 if (ln.kmax <= 2) k_tile_sweep_c64<2><<<(unsigned)nb, kThreads, sm64, s->stream>>>((float2*)s->state, d, t0);
@@ -1116,6 +1127,15 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         s->stats.bytes_moved += 2.0 * esz * (double)s->len;
     }
     return bs_cuda_check(s, cudaGetLastError(), "tile sweep launch");
+}
+
+void bs_collect_tc_time(bs_sim* s) {
+    for (size_t i = 0; i < s->tc_events_used; i++) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, s->tc_events[2 * i], s->tc_events[2 * i + 1]) == cudaSuccess)
+            s->stats.tc_ms += ms;
+    }
+    s->tc_events_used = 0;
 }
 
 int bs_check_device_flag(bs_sim* s) {

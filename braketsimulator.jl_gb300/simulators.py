@@ -165,7 +165,8 @@ class AbstractSimulator:
         st = _abi.BsStats()
         self._h.call("bs_last_stats", C.byref(st))
         return {"sweeps": st.sweeps, "kernel_launches": st.kernel_launches, "gates": st.gates,
-                "bytes_moved": st.bytes_moved, "gpu_ms": st.gpu_ms, "tc_gates": st.tc_gates}
+                "bytes_moved": st.bytes_moved, "gpu_ms": st.gpu_ms, "tc_gates": st.tc_gates,
+                "tc_launches": st.tc_launches, "tc_ms": st.tc_ms}
 
     # ---- state
     def _get(self) -> np.ndarray:

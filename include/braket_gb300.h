@@ -80,6 +80,8 @@ typedef struct bs_stats {
     double  bytes_moved;       /* algorithmic HBM bytes of the executed sweeps */
     double  gpu_ms;            /* device time of the call (CUDA events) */
     int64_t tc_gates;          /* fused unitaries applied on the tensor cores (each replacing a run of gates) */
+    int64_t tc_launches;       /* tensor-core sweep kernel launches */
+    double  tc_ms;             /* their device time (CUDA events around each launch, same stream) */
 } bs_stats;
 
 /* ---- lifecycle: StateVectorSimulator(T, n, shots) / DensityMatrixSimulator(T, n, shots)

@@ -61,3 +61,17 @@ def test_adjoint_other_generators_and_shared_parameters():
     pidx = [-1] * n + [0, 1, 2, 3, -1, 0]
     e2, g2 = adj.adjoint_gradient(sim, ops, h, pidx)
     assert abs(g2[0] - (g[0] + g[4])) < 1e-12
+
+
+@pytest.mark.parametrize("n", [6, 13])
+def test_adjoint_complex64_state(n):
+    """complex64 state, float-float arithmetic and FP64-grade inner products: the gradient differs
+    from the complex128 one by the complex64 rounding of the stored states only."""
+    rng = np.random.default_rng(60 + n)
+    ops = ansatz(n, 3, rng)
+    h = hamiltonian(n, 10, rng)
+    e128, g128 = adj.adjoint_gradient(bs.StateVectorSimulator(n, 0), ops, h)
+    e64, g64 = adj.adjoint_gradient(bs.StateVectorSimulator(n, 0, precision="c64"), ops, h)
+    scale = max(1.0, sum(abs(c) for c, _ in h))
+    assert abs(e64 - e128) < 2e-5 * scale
+    assert np.max(np.abs(g64 - g128)) < 2e-5 * scale
