@@ -35,13 +35,15 @@ bool is_plain_cz(const HostGate& g) {
            g.mat[3] == 0.0 && __builtin_popcountll(g.cmask) == 1 && g.cval == g.cmask;
 }
 
-// Apply a canonical gate to a 32-amplitude vector over the block bits.  pos[e]: block bit of
-// endian bit e, or -1 for a uniform bit whose value is (uval >> e) & 1.
-void apply_block(const HostGate& g, const int* pos, uint64_t uval, cd* v) {
-    // controls: in-block ones become an index condition, uniform ones decide whether the gate acts
+// Left-multiply the 32x32 block matrix U (row r, column c at U[r * 32 + c]) by a canonical gate.
+// pos[e]: block bit of endian bit e, or -1 for a uniform bit whose value is (uval >> e) & 1.
+void apply_block(const HostGate& g, const int* pos, uint64_t uval, cd* U) {
+    // controls: in-block ones become a row-index condition, uniform ones decide whether the gate acts
     uint32_t cm = 0, cv = 0;
-    for (int e = 0; e < 64; e++) {
-        if (!((g.cmask >> e) & 1ULL)) continue;
+    uint64_t rest = g.cmask;
+    while (rest) {
+        const int e = __builtin_ctzll(rest);
+        rest &= rest - 1;
         const uint64_t want = (g.cval >> e) & 1ULL;
         if (pos[e] < 0) {
             if (((uval >> e) & 1ULL) != want) return;
@@ -52,43 +54,55 @@ void apply_block(const HostGate& g, const int* pos, uint64_t uval, cd* v) {
     }
     const int D = 1 << g.k;
     if (g.kind == 1) {
-        // diagonal: target bits may be uniform (constant over the block)
-        for (uint32_t i = 0; i < 32; i++) {
-            if ((i & cm) != cv) continue;
+        // diagonal: target bits may be uniform (constant over the block); row r scales by d[index(r)]
+        for (uint32_t r = 0; r < 32; r++) {
+            if ((r & cm) != cv) continue;
             int di = 0;
             for (int q = 0; q < g.k; q++) {
                 const int e = g.ebit[q];
-                const int bit = pos[e] >= 0 ? (int)((i >> pos[e]) & 1u) : (int)((uval >> e) & 1ULL);
+                const int bit = pos[e] >= 0 ? (int)((r >> pos[e]) & 1u) : (int)((uval >> e) & 1ULL);
                 di |= bit << q;
             }
-            v[i] *= cd(g.mat[2 * di], g.mat[2 * di + 1]);
+            const double dr = g.mat[2 * di], dim = g.mat[2 * di + 1];
+            for (int c = 0; c < 32; c++) {
+                const double ur = U[r * 32 + c].real(), ui = U[r * 32 + c].imag();
+                U[r * 32 + c] = cd(dr * ur - dim * ui, dr * ui + dim * ur);
+            }
         }
         return;
     }
-    int tb[BS_MAX_TARGETS];
+    uint32_t off[32];
     uint32_t tmask = 0;
-    for (int q = 0; q < g.k; q++) { tb[q] = pos[g.ebit[q]]; tmask |= 1u << tb[q]; }
-    auto dep = [&](int c) {
+    for (int q = 0; q < g.k; q++) tmask |= 1u << pos[g.ebit[q]];
+    for (int c = 0; c < D; c++) {
         uint32_t j = 0;
-        for (int q = 0; q < g.k; q++) if ((c >> q) & 1) j |= 1u << tb[q];
-        return j;
-    };
+        for (int q = 0; q < g.k; q++) if ((c >> q) & 1) j |= 1u << pos[g.ebit[q]];
+        off[c] = j;
+    }
+    static const cd ipow[4] = {cd(1, 0), cd(0, 1), cd(-1, 0), cd(0, -1)};
+    cd x[32], y[32];
     for (uint32_t i = 0; i < 32; i++) {
         if (i & tmask) continue;
         if ((i & cm) != cv) continue;
-        cd x[32], y[32];
-        for (int c = 0; c < D; c++) x[c] = v[i | dep(c)];
-        if (g.kind == 0) {
-            for (int r = 0; r < D; r++) {
-                cd s = 0;
-                for (int c = 0; c < D; c++) s += cd(g.mat[2 * (r * D + c)], g.mat[2 * (r * D + c) + 1]) * x[c];
-                y[r] = s;
+        for (int col = 0; col < 32; col++) {
+            for (int c = 0; c < D; c++) x[c] = U[(i | off[c]) * 32 + col];
+            if (g.kind == 0) {
+                // plain real arithmetic (std::complex products go through a NaN-checking library call)
+                for (int r = 0; r < D; r++) {
+                    double sr = 0, si = 0;
+                    const double* mr = g.mat.data() + 2 * r * D;
+                    for (int c = 0; c < D; c++) {
+                        const double ar = mr[2 * c], ai = mr[2 * c + 1], xr = x[c].real(), xi = x[c].imag();
+                        sr += ar * xr - ai * xi;
+                        si += ar * xi + ai * xr;
+                    }
+                    y[r] = cd(sr, si);
+                }
+            } else {
+                for (int c = 0; c < D; c++) y[g.perm[2 * c]] = ipow[g.perm[2 * c + 1] & 3] * x[c];
             }
-        } else {
-            static const cd ipow[4] = {cd(1, 0), cd(0, 1), cd(-1, 0), cd(0, -1)};
-            for (int c = 0; c < D; c++) y[g.perm[2 * c]] = ipow[g.perm[2 * c + 1] & 3] * x[c];
+            for (int r = 0; r < D; r++) U[(i | off[r]) * 32 + col] = y[r];
         }
-        for (int r = 0; r < D; r++) v[i | dep(r)] = y[r];
     }
 }
 
@@ -152,15 +166,12 @@ void bs_fuse_tc(const std::vector<HostGate>& in, const int* local, int T, std::v
             uint64_t uval = 0;
             for (size_t i = 0; i < f.ubits.size(); i++) if ((var >> i) & 1) uval |= 1ULL << f.ubits[i];
             double* m = f.mat.data() + (size_t)var * 2048;
-            for (int c = 0; c < 32; c++) {
-                cd v[32];
-                for (int r = 0; r < 32; r++) v[r] = 0;
-                v[c] = 1;
-                for (int i : b.idx) apply_block(in[(size_t)i], pos, uval, v);
-                for (int r = 0; r < 32; r++) {
-                    m[2 * (r * 32 + c)] = v[r].real();
-                    m[2 * (r * 32 + c) + 1] = v[r].imag();
-                }
+            std::vector<cd> U(32 * 32, cd(0, 0));
+            for (int r = 0; r < 32; r++) U[(size_t)r * 33] = 1;
+            for (int i : b.idx) apply_block(in[(size_t)i], pos, uval, U.data());
+            for (int r = 0; r < 32 * 32; r++) {
+                m[2 * r] = U[(size_t)r].real();
+                m[2 * r + 1] = U[(size_t)r].imag();
             }
         }
         out.push_back(std::move(f));
@@ -274,34 +285,5 @@ bool bs_tc_exponent(const double* mat, int n_mat, int& eu) {
     if (mx > 0) std::frexp(mx, &e);          // mx < 2^e
     if (e > 12) return false;
     eu = std::max(e, -60);
-    return true;
-}
-
-bool bs_tc_digits(const double* mat, uint16_t* dst, int eu) {
-    // real embedding: n = 2 t' + c' (output re/im), k = 2 t + c (input re/im); entries below 2^eu
-    std::vector<double> ur(64 * 64);
-    for (int tp = 0; tp < 32; tp++)
-        for (int t = 0; t < 32; t++) {
-            const double re = mat[2 * (tp * 32 + t)], im = mat[2 * (tp * 32 + t) + 1];
-            ur[(2 * tp) * 64 + 2 * t] = re;
-            ur[(2 * tp) * 64 + 2 * t + 1] = -im;
-            ur[(2 * tp + 1) * 64 + 2 * t] = im;
-            ur[(2 * tp + 1) * 64 + 2 * t + 1] = re;
-        }
-    // six balanced digits d_i in [-128, 128]: u 2^(7-eu) = sum_i d_i 2^(-8 i); slice i holds d_i 2^(-8 i) as bf16
-    for (int n = 0; n < 64; n++)
-        for (int k = 0; k < 64; k++) {
-            double v = std::ldexp(ur[n * 64 + k], 7 - eu);
-            if (!(std::fabs(v) < 128.0)) return false;
-            for (int i = 0; i < 6; i++) {
-                const double d = std::nearbyint(v);
-                v = (v - d) * 256.0;
-                const float f = std::ldexp((float)d, -8 * i);   // exact: |d| <= 128
-                uint32_t bits;
-                std::memcpy(&bits, &f, 4);
-                const int s = k / 16, kc = (k % 16) / 8, rg = n / 8, r = n % 8, el = k % 8;
-                dst[(size_t)(i * 4 + s) * 1024 + rg * 128 + kc * 64 + r * 8 + el] = (uint16_t)(bits >> 16);
-            }
-        }
     return true;
 }

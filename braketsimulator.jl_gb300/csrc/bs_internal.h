@@ -121,9 +121,6 @@ bool bs_tc_enabled();
 // Fold runs of in-tile gates into kind-4 HostGates (5 endian bits, 32x32 matrix) where that is cheaper.
 // local[e]: tile position of endian bit e or -1.
 void bs_fuse_tc(const std::vector<HostGate>& in, const int* local, int T, std::vector<HostGate>& out);
-// Six bf16 digit slices of the 64x64 real embedding of a 32x32 matrix, in the shared-memory
-// operand layout (24576 values); eu: entries are below 2^eu.  False if not representable.
-bool bs_tc_digits(const double* mat, uint16_t* dst, int eu);
 // Smallest eu with every entry of the n_mat 32x32 matrices below 2^eu; false if not finite or above 2^12.
 bool bs_tc_exponent(const double* mat, int n_mat, int& eu);
 

@@ -9,7 +9,9 @@
 // kernels src/custom_gates.jl:364-416; the density-matrix gate of
 // src/dm_simulator.jl:130-140 is two tile gates (column bits U, row bits conj U).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
+#include <thread>
 #include "bs_internal.h"
 #include "bs_ff.cuh"
 #include "bs_tc.cuh"
@@ -331,6 +333,37 @@ __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ 
     for (int i = 0; i < 16; i++) {
         const int j = i * 256 + (int)threadIdx.x;
         __stcs(psi + (base | ((int64_t)off32[j >> L] << L) | (int64_t)(j & lowmask)), store_c128(f4c(smem[tc::sw(j)])));
+    }
+}
+
+// Digit slices of the fused matrices for the tensor-core sweep, one CTA per matrix variant.
+// mats: complex 32x32 row-major FP64 per variant; scale[v] = 2^(7 - eu) of the variant's gate.
+// Entry (n, k) of the real 64x64 embedding (n = 2t'+c' output re/im, k = 2t+c input re/im) is split
+// into six balanced digits d_i in [-128, 128] (u 2^(7-eu) = sum_i d_i 2^(-8i), each digit rounded to
+// nearest even), digit i stored as the bf16 of d_i 2^(-8i) at its place in the K-major no-swizzle
+// operand layout (per digit and k-step a 2 KiB block of 8x8 core matrices: row group n/8 at 256 B,
+// K half at 128 B, row n%8 at 16 B).
+__global__ void __launch_bounds__(256) k_tc_digits(const double* __restrict__ mats, const double* __restrict__ scale,
+                                                   uint16_t* __restrict__ pool) {
+    const int v = blockIdx.x;
+    const double* m = mats + (size_t)v * 2048;
+    uint16_t* dst = pool + (size_t)v * tc::kPoolBlock;
+    const double sc = scale[v];
+    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+        const int n = e >> 6, k = e & 63;
+        const int tp = n >> 1, cp = n & 1, t = k >> 1, c = k & 1;
+        const double re = m[2 * (tp * 32 + t)], im = m[2 * (tp * 32 + t) + 1];
+        const double u = (cp == c) ? re : (cp == 0 ? -im : im);
+        double x = u * sc;
+        const int s = k >> 4, kc = (k >> 3) & 1, rg = n >> 3, r = n & 7, el = k & 7;
+        const int pos = rg * 128 + kc * 64 + r * 8 + el;
+#pragma unroll
+        for (int i = 0; i < 6; i++) {
+            const double d = rint(x);
+            x = (x - d) * 256.0;
+            const float f = __double2float_rn(d) * __int_as_float((127 - 8 * i) << 23);   // exact: |d| <= 128
+            dst[(size_t)(i * 4 + s) * 1024 + pos] = (uint16_t)(__float_as_uint(f) >> 16);
+        }
     }
 }
 
@@ -832,15 +865,47 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     };
     std::vector<Launch> launches;
     std::vector<int32_t> big_bits;
-    std::vector<uint16_t> tc_pool;
+    std::vector<double> tc_mats, tc_scale;   // fused matrices (complex 32x32 per variant), 2^(7-eu) per variant
+    int64_t n_var = 0;
     const bool c64 = s->precision == BS_PREC_C64;
-    // measured on GB300: fused tensor-core sweeps win from 27 vector bits up and lose below
-    // (per-CTA overheads over too few tiles); BS_TC_MIN_BITS overrides the threshold
+    // fused tensor-core sweeps from 22 vector bits up (measured wins at 24, 26, 28 and 30 bits;
+    // small states are dominated by host planning); BS_TC_MIN_BITS overrides the threshold
     const char* tmb = getenv("BS_TC_MIN_BITS");
-    const int tc_min_bits = tmb ? atoi(tmb) : 27;
+    const int tc_min_bits = tmb ? atoi(tmb) : 22;
     const bool use_tc = bs_tc_enabled() && !c64 && T == 12 && L == 5 && n_bits >= tc_min_bits;
-    std::vector<HostGate> fused;
+    // fusion per sweep (independent, so on a few host threads); a sweep left with unfused 3/4-target
+    // gates keeps its plain gate list, since the tensor-core sweep kernel carries float-float paths for
+    // 1- and 2-target gates only
+    std::vector<std::vector<HostGate>> fused_all(use_tc ? sweeps.size() : 0);
+    std::vector<char> fused_ok(fused_all.size(), 0);
+    if (use_tc) {
+        auto work = [&](size_t first, size_t step) {
+            for (size_t i = first; i < sweeps.size(); i += step) {
+                const Sweep& sw = sweeps[i];
+                if ((int)sw.hi_bits.size() != T - L) continue;
+                int local[64];
+                for (int b = 0; b < 64; b++) local[b] = -1;
+                for (int b = 0; b < L; b++) local[b] = b;
+                for (size_t q = 0; q < sw.hi_bits.size(); q++) local[sw.hi_bits[q]] = L + (int)q;
+                bs_fuse_tc(sw.gates, local, T, fused_all[i]);
+                bool ok = true;
+                for (const HostGate& hg : fused_all[i]) if (hg.kind != 1 && hg.kind != 4 && hg.k >= 3) ok = false;
+                fused_ok[i] = ok;
+            }
+        };
+        const unsigned hw = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+        const size_t nth = std::min<size_t>(sweeps.size(), hw);
+        if (nth <= 1) {
+            work(0, 1);
+        } else {
+            std::vector<std::thread> th;
+            for (size_t t = 0; t < nth; t++) th.emplace_back(work, t, nth);
+            for (std::thread& x : th) x.join();
+        }
+    }
+    size_t swi = 0;
     for (const Sweep& sw : sweeps) {
+        const size_t si = swi++;
         Launch ln;
         ln.gate0 = (int64_t)tg.size();
         ln.n_gates = 0;
@@ -852,14 +917,7 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         for (int b = 0; b < 64; b++) local[b] = -1;
         for (int b = 0; b < L; b++) local[b] = b;
         for (size_t i = 0; i < sw.hi_bits.size(); i++) local[sw.hi_bits[i]] = L + (int)i;
-        const std::vector<HostGate>* glist = &sw.gates;
-        if (use_tc && (int)sw.hi_bits.size() == T - L) {
-            bs_fuse_tc(sw.gates, local, T, fused);
-            // the tensor-core sweep kernel carries float-float paths for 1- and 2-target gates only
-            bool ok = true;
-            for (const HostGate& hg : fused) if (hg.kind != 1 && hg.kind != 4 && hg.k >= 3) ok = false;
-            if (ok) glist = &fused;
-        }
+        const std::vector<HostGate>* glist = (use_tc && fused_ok[si]) ? &fused_all[si] : &sw.gates;
         for (const HostGate& hg : *glist) {
             if (hg.kind == 4) {
                 TileGate t{};
@@ -869,13 +927,13 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
                 const int nvar = 1 << hg.ubits.size();
                 t.tc_nu = (int32_t)hg.ubits.size();
                 for (size_t i = 0; i < hg.ubits.size(); i++) t.tc_ub[i] = hg.ubits[i];
-                t.tc_off = (int32_t)(tc_pool.size() / tc::kPoolBlock);
-                tc_pool.resize(tc_pool.size() + (size_t)nvar * tc::kPoolBlock);
+                t.tc_off = (int32_t)n_var;
                 int eu = 0;
-                bool ok = bs_tc_exponent(hg.mat.data(), nvar, eu);
-                for (int v = 0; v < nvar && ok; v++)
-                    ok = bs_tc_digits(hg.mat.data() + (size_t)v * 2048, tc_pool.data() + (size_t)(t.tc_off + v) * tc::kPoolBlock, eu);
-                if (!ok) return bs_fail(s, BS_ERR_INVALID_ARG, "fused gate matrix out of range");
+                if (!bs_tc_exponent(hg.mat.data(), nvar, eu))
+                    return bs_fail(s, BS_ERR_INVALID_ARG, "fused gate matrix out of range");
+                tc_mats.insert(tc_mats.end(), hg.mat.begin(), hg.mat.begin() + (size_t)nvar * 2048);
+                for (int v = 0; v < nvar; v++) tc_scale.push_back(std::ldexp(1.0, 7 - eu));
+                n_var += nvar;
                 t.tc_eu = eu;
                 ln.tc_last = ln.n_gates;
                 ln.n_tc++;
@@ -992,12 +1050,17 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     int64_t b_m = al((int64_t)mats.size() * (int64_t)sizeof(float4));
     int64_t b_p = al((int64_t)(perms.size() + big_bits.size() + 1) * (int64_t)sizeof(int32_t));
     int64_t b_s = al((int64_t)(segs.size() + 1) * (int64_t)sizeof(RBSeg));
-    int64_t b_tc = al((int64_t)tc_pool.size() * (int64_t)sizeof(uint16_t));
-    int rc = bs_ensure_plan(s, b_tg + b_m + b_p + b_s + b_tc);
+    int64_t b_tm = al((int64_t)tc_mats.size() * (int64_t)sizeof(double));
+    int64_t b_ts = al((int64_t)tc_scale.size() * (int64_t)sizeof(double));
+    int64_t b_tc = al(n_var * tc::kPoolBlock * (int64_t)sizeof(uint16_t));   // written on the device
+    const int64_t o_tm = b_tg + b_m + b_p + b_s, o_ts = o_tm + b_tm, o_tc = o_ts + b_ts;
+    int rc = bs_ensure_plan(s, o_tc + b_tc);
     if (rc) return rc;
-    std::vector<char> host((size_t)(b_tg + b_m + b_p + b_s + b_tc), 0);
-    if (!tc_pool.empty())
-        std::memcpy(host.data() + b_tg + b_m + b_p + b_s, tc_pool.data(), tc_pool.size() * sizeof(uint16_t));
+    std::vector<char> host((size_t)o_tc, 0);
+    if (!tc_mats.empty()) {
+        std::memcpy(host.data() + o_tm, tc_mats.data(), tc_mats.size() * sizeof(double));
+        std::memcpy(host.data() + o_ts, tc_scale.data(), tc_scale.size() * sizeof(double));
+    }
     if (!segs.empty()) std::memcpy(host.data() + b_tg + b_m + b_p, segs.data(), segs.size() * sizeof(RBSeg));
     if (!tg.empty()) std::memcpy(host.data(), tg.data(), tg.size() * sizeof(TileGate));
     if (!mats.empty()) std::memcpy(host.data() + b_tg, mats.data(), mats.size() * sizeof(float4));
@@ -1038,8 +1101,10 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         attr_set[s->device & 63] = true;
     }
     double2* psi = (double2*)s->state;
-    const uint16_t* d_tc = (const uint16_t*)(dev + b_tg + b_m + b_p + b_s);
-    if (!tc_pool.empty()) {
+    uint16_t* d_tc = (uint16_t*)(dev + o_tc);
+    if (n_var) {
+        k_tc_digits<<<(unsigned)n_var, 256, 0, s->stream>>>((const double*)(dev + o_tm), (const double*)(dev + o_ts), d_tc);
+        s->stats.kernel_launches++;
         if (!s->dev_flag) {
             rc = bs_cuda_check(s, cudaMalloc((void**)&s->dev_flag, 256), "flag alloc");
             if (rc) return rc;

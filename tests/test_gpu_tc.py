@@ -16,7 +16,7 @@ TOL = 1e-12
 
 class tc_mode:
     """BS_TC=0 keeps every gate on the float-float tile path; BS_TC_MIN_BITS lowers the state size
-    from which fused tensor-core sweeps are used (27 vector bits by default) so that oracle-sized
+    from which fused tensor-core sweeps are used (22 vector bits by default) so that oracle-sized
     cases exercise them.  Both are read on every evolve."""
 
     def __init__(self, on):
