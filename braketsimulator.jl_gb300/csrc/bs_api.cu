@@ -291,6 +291,10 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
             unsigned mode = (op.flags & BS_NOISE_PHYSICAL) ? BS_NOISE_PHYSICAL : noise_mode;
             if (mode & BS_NOISE_PHYSICAL) {
                 rc = bs_lower_kraus_physical(s, op.matrix, op.n_matrices, op.n_targets, op.targets, op.flags, pending);
+            } else if (s->precision == BS_PREC_C128 && op.n_targets <= 2) {
+                // inside the sweeps (complex128 tile kernels)
+                rc = bs_lower_kraus_reference(s, op.matrix, op.n_matrices, op.n_targets, op.targets, op.flags,
+                                              pending);
             } else {
                 rc = flush();
                 if (!rc) rc = bs_kraus_reference(s, op.matrix, op.n_matrices, op.n_targets, op.targets, op.flags);

@@ -133,6 +133,37 @@ __global__ void k_kraus_ref_big(ST* __restrict__ S, int n, int k, const int* __r
 
 }  // namespace
 
+// A 1- or 2-target channel in the reference's update rule as a tile gate of a density-matrix sweep
+// (kind 5): ebit[0..k-1] are the row endian bits of the targets (matrix bit j <-> ebit[j], the
+// canonical order of bs_kraus_reference), ebit[k..2k-1] the column endian bits; mat holds the nk
+// Kraus matrices, row-major D x D complex each.
+int bs_lower_kraus_reference(bs_sim* s, const double* kraus, int nk, int k, const int* targets, unsigned flags,
+                             std::vector<HostGate>& out) {
+    if (s->kind != BS_KIND_DM) return bs_fail(s, BS_ERR_STATE, "noise needs a density-matrix simulator");
+    if (k < 1 || k > 2) return bs_fail(s, BS_ERR_INVALID_ARG, "in-sweep reference channels take 1 or 2 targets");
+    if (nk < 1 || !kraus) return bs_fail(s, BS_ERR_INVALID_ARG, "no Kraus matrices");
+    uint64_t seen = 0;
+    for (int i = 0; i < k; i++) {
+        if (targets[i] < 0 || targets[i] >= s->n) return bs_fail(s, BS_ERR_INVALID_ARG, "target qubit out of range");
+        if ((seen >> targets[i]) & 1ULL) return bs_fail(s, BS_ERR_INVALID_ARG, "repeated qubit");
+        seen |= 1ULL << targets[i];
+    }
+    std::vector<int> ct(targets, targets + k);
+    if (flags & BS_GATE_SORTED_TARGETS) std::sort(ct.begin(), ct.end(), [](int a, int b) { return a > b; });
+    else if (flags & BS_GATE_MSB_FIRST) std::reverse(ct.begin(), ct.end());
+    HostGate g;
+    g.kind = 5;
+    g.k = k;
+    for (int j = 0; j < k; j++) {
+        g.ebit[j] = s->n - 1 - ct[(size_t)j];
+        g.ebit[k + j] = g.ebit[j] + s->n;
+    }
+    const int D = 1 << k;
+    g.mat.assign(kraus, kraus + (size_t)nk * D * D * 2);
+    out.push_back(std::move(g));
+    return BS_OK;
+}
+
 int bs_kraus_reference(bs_sim* s, const double* kraus, int nk, int k, const int* targets, unsigned flags) {
     if (s->kind != BS_KIND_DM) return bs_fail(s, BS_ERR_STATE, "noise needs a density-matrix simulator");
     if (k < 1 || k > BS_MAX_TARGETS) return bs_fail(s, BS_ERR_INVALID_ARG, "channel needs 1..10 targets");

@@ -188,6 +188,13 @@ void bs_fuse_tc(const std::vector<HostGate>& in, const int* local, int T, std::v
     };
     for (size_t i = 0; i < in.size(); i++) {
         const HostGate& g = in[i];
+        if (g.kind == 5) {
+            // a reference-rule channel commutes with nothing: every open block closes before it
+            for (Block& b : open) emit(b);
+            open.clear();
+            out.push_back(g);
+            continue;
+        }
         // tile bits and uniform bits of the gate; dense and monomial targets must be in the tile
         uint64_t bits = 0, ub = 0;
         bool fusable = g.kind <= 2 && g.k <= 5;

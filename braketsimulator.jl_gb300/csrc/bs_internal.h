@@ -17,6 +17,8 @@
 //   kind 3: a run of CZ gates applied as one parity phase (npar, pshift, pmask)
 //   kind 4: fused dense unitary on 5 tile-local bits gbit[0..4] (matrix bit j <-> gbit[j]),
 //           applied on the tensor cores from the bf16 digit slices at tc_off (48 KiB blocks)
+//   kind 5: Kraus channel on k <= 2 targets in the reference's block-diagonal update rule
+//           (density matrix): tbit[0..2k-1] row then column target bits, pmask[0..1], npar = nk
 // Controls: (tile_index & lc_mask) == lc_val for in-tile controls,
 //           (global_base & gc_mask) == gc_val for controls outside the tile.
 struct TileGate {
@@ -53,7 +55,8 @@ struct SweepDesc {
 };
 
 struct HostGate {                // a gate after lowering to the canonical convention
-    int kind;                    // 0 dense, 1 diagonal, 2 monomial, 4 fused 5-bit unitary
+    int kind;                    // 0 dense, 1 diagonal, 2 monomial, 4 fused 5-bit unitary,
+                                 // 5 reference-rule Kraus channel (ebit: k row bits, then k column bits)
     int k;
     int ebit[BS_MAX_TARGETS];    // endian bit of target j (matrix bit j)
     std::vector<double> mat;     // interleaved complex; dense 4^k*2, diag 2^k*2
@@ -134,3 +137,6 @@ void bs_collect_tc_time(bs_sim* s);
 // ---- reference-compat Kraus (bs_dm.cu)
 int bs_kraus_reference(bs_sim* s, const double* kraus, int nk, int k, const int* targets,
                        unsigned flags);
+// The same channel (1 or 2 targets) as a kind-5 HostGate applied inside a sweep.
+int bs_lower_kraus_reference(bs_sim* s, const double* kraus, int nk, int k, const int* targets, unsigned flags,
+                             std::vector<HostGate>& out);

@@ -202,7 +202,10 @@ void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, std::vector<
     const size_t G = gates.size();
     std::vector<char> done(G, 0);
     size_t remaining = G, first = 0;
+    // kind 5 (reference-rule channel) acts on the elements whose row and column agree on every other
+    // bit: it commutes with nothing, so it touches every bit, and it needs its row and column bits
     auto touch = [&](const HostGate& g) {
+        if (g.kind == 5) return ~(uint64_t)0;
         uint64_t m = g.cmask;
         for (int q = 0; q < g.k; q++) m |= 1ULL << g.ebit[q];
         return m;
@@ -210,7 +213,8 @@ void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, std::vector<
     auto need = [&](const HostGate& g) {
         uint64_t m = 0;
         if (g.kind == 1) return m;
-        for (int q = 0; q < g.k; q++) if (g.ebit[q] >= L) m |= 1ULL << g.ebit[q];
+        const int nb = g.kind == 5 ? 2 * g.k : g.k;
+        for (int q = 0; q < nb; q++) if (g.ebit[q] >= L) m |= 1ULL << g.ebit[q];
         return m;
     };
     while (remaining) {

@@ -112,12 +112,42 @@ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
     return x ^ (x >> 31);
 }
 
+// The same search by a whole warp: block by binary search, then 32 probabilities per step with a
+// warp prefix sum and a ballot for the first running sum >= t (the prefix associates differently
+// from a left-to-right sum, so only exact boundary ties can land on a neighbouring index).
+__device__ int64_t cdf_find_warp(const double2* st, int dm, int64_t dim, const double* incl, int64_t nb, double t) {
+    const int lane = threadIdx.x & 31;
+    int64_t lo = 0, hi = nb - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (incl[mid] >= t) hi = mid; else lo = mid + 1;
+    }
+    double cw = (lo == 0) ? 0.0 : incl[lo - 1];
+    const int64_t end = std::min<int64_t>(dim, (lo + 1) * kBlk);
+    for (int64_t c = lo * kBlk; c < end; c += 32) {
+        const int64_t i = c + lane;
+        double p = (i < end) ? prob_at(st, dm, dim, i) : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double v = __shfl_up_sync(0xffffffffu, p, o);
+            if (lane >= o) p += v;
+        }
+        const unsigned hit = __ballot_sync(0xffffffffu, i < end && cw + p >= t);
+        if (hit) return c + __ffs(hit) - 1;
+        cw += __shfl_sync(0xffffffffu, p, 31);
+    }
+    return end - 1;
+}
+
+// one shot per warp; uniforms from a counter-based splitmix64 stream
 __global__ void k_sample_rng(const double2* __restrict__ st, int dm, int64_t dim, const double* __restrict__ incl,
                              int64_t nb, uint64_t seed, int64_t shots, int64_t* __restrict__ out) {
-    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < shots; s += (int64_t)gridDim.x * blockDim.x) {
-        uint64_t r = splitmix64(seed ^ splitmix64((uint64_t)s));
-        double u = (double)(r >> 11) * 0x1.0p-53;
-        out[s] = cdf_find(st, dm, dim, incl, nb, u * incl[nb - 1]);
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; s < shots; s += warps) {
+        const uint64_t r = splitmix64(seed ^ splitmix64((uint64_t)s));
+        const double u = (double)(r >> 11) * 0x1.0p-53;
+        const int64_t v = cdf_find_warp(st, dm, dim, incl, nb, u * incl[nb - 1]);
+        if ((threadIdx.x & 31) == 0) out[s] = v;
     }
 }
 
@@ -329,7 +359,7 @@ int bs_sample(bs_sim* s, uint64_t seed, int64_t shots, int64_t* out) {
     if (rc) return rc;
     int64_t* dout = (int64_t*)buf;
     const int64_t dim = (int64_t)1 << s->n;
-    k_sample_rng<<<grid(shots, 128), 128, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, incl, nb,
+    k_sample_rng<<<grid(shots * 32, 128), 128, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, incl, nb,
                                                             seed, shots, dout);
     cudaMemcpyAsync(out, dout, (size_t)shots * 8, cudaMemcpyDeviceToHost, s->stream);
     cudaFreeAsync(buf, s->stream);

@@ -163,6 +163,78 @@ __device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const flo
     }
 }
 
+// Kraus channel on K <= 2 targets in the reference's update rule (src/noise_kernels.jl:105-168): the
+// stored matrix S gets B <- sum_q K_q B K_q^dagger on every D x D block B whose row and column agree on
+// all non-target bits (vec(S) index = row + column 2^n); other elements are left alone.  tbit[0..K-1]:
+// tile positions of the row target bits (matrix bit j <-> tbit[j]), tbit[K..2K-1]: of the column
+// target bits; pmask[0]: row-index mask of the non-target bits; pmask[1]: the non-target bits whose
+// row and column bits both lie outside the tile (so that part of the test is uniform in the CTA);
+// npar: number of Kraus matrices, row-major D x D each at mat_off.
+template <int K, bool SW, typename OT>
+__device__ void tile_kraus_ref(float4* sm, int T, int L, const TileGate& g, const float4* __restrict__ mats,
+                               int64_t base, const OT* off_tab, int osh, int n) {
+    constexpr int D = 1 << K;
+    const int64_t rmask = ((int64_t)1 << n) - 1;
+    if ((((base & rmask) ^ (base >> n)) & (int64_t)g.pmask[1]) != 0) return;
+    int pos[2 * K];
+#pragma unroll
+    for (int q = 0; q < 2 * K; q++) pos[q] = g.tbit[q];
+#pragma unroll
+    for (int a = 0; a < 2 * K; a++)
+#pragma unroll
+        for (int b = a + 1; b < 2 * K; b++)
+            if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
+    const int lowmask = (1 << L) - 1;
+    const float4* km = mats + g.mat_off;
+    for (int b = threadIdx.x; b < (1 << (T - 2 * K)); b += blockDim.x) {
+        int j0 = b;
+#pragma unroll
+        for (int q = 0; q < 2 * K; q++) j0 = insert0(j0, pos[q]);
+        const int64_t gi = base | ((int64_t)off_tab[j0 >> L] << osh) | (int64_t)(j0 & lowmask);
+        if ((((gi & rmask) ^ (gi >> n)) & (int64_t)g.pmask[0]) != 0) continue;
+        // rho[r][c]: row target pattern r, column target pattern c
+        cff rho[D][D];
+        int idx[D][D];
+#pragma unroll
+        for (int r = 0; r < D; r++)
+#pragma unroll
+            for (int c = 0; c < D; c++) {
+                int j = j0;
+#pragma unroll
+                for (int q = 0; q < K; q++) {
+                    if ((r >> q) & 1) j |= 1 << g.tbit[q];
+                    if ((c >> q) & 1) j |= 1 << g.tbit[K + q];
+                }
+                idx[r][c] = sx<SW>(j);
+                rho[r][c] = f4c(sm[idx[r][c]]);
+            }
+        // out[i][j] = sum_q sum_c (sum_r K_q[i][r] rho[r][c]) conj(K_q[j][c]), one element at a time
+#pragma unroll 1
+        for (int i = 0; i < D; i++)
+#pragma unroll 1
+            for (int j = 0; j < D; j++) {
+                ffacc ar{0.f, 0.f}, ai{0.f, 0.f};
+                bool first = true;
+                for (int q = 0; q < g.npar; q++) {
+                    const float4* Kq = km + q * D * D;
+#pragma unroll
+                    for (int c = 0; c < D; c++) {
+                        ffacc tr, ti;
+                        cmac_first(tr, ti, f4c(__ldg(Kq + i * D)), rho[0][c]);
+#pragma unroll
+                        for (int r = 1; r < D; r++) cmac(tr, ti, f4c(__ldg(Kq + i * D + r)), rho[r][c]);
+                        const cff t = cdone(tr, ti);
+                        const float4 kj = __ldg(Kq + j * D + c);
+                        const cff kc = {kj.x, kj.y, -kj.z, -kj.w};
+                        if (first) { cmac_first(ar, ai, kc, t); first = false; }
+                        else cmac(ar, ai, kc, t);
+                    }
+                }
+                sm[idx[i][j]] = c4f(cdone(ar, ai));
+            }
+    }
+}
+
 // KMAX: widest dense/monomial gate of the sweep (2 or 4); narrow sweeps get a
 // kernel with fewer live registers and therefore more resident warps.
 template <int KMAX, int NT>
@@ -204,6 +276,9 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
             }
         } else if (kind == 1) {
             tile_diag(smem, T, L, g, d.mats, base, off_tab, 0);
+        } else if (kind == 5) {
+            if (k == 1) tile_kraus_ref<1, false>(smem, T, L, g, d.mats, base, off_tab, 0, d.n_bits / 2);
+            else if (KMAX > 2) tile_kraus_ref<2, false>(smem, T, L, g, d.mats, base, off_tab, 0, d.n_bits / 2);
         } else if (kind == 0) {
             if (k == 1) tile_dense<1>(smem, T, g, d.mats);
             else if (k == 2 || KMAX == 2) tile_dense<2>(smem, T, g, d.mats);
@@ -310,6 +385,7 @@ __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ 
             }
         } else if (kind == 1) {
             tile_diag<uint32_t, true>(smem, T, L, g, d.mats, base, off32, L);
+
         } else if (kind == 0) {   // the planner routes sweeps with unfused 3- or 4-target gates elsewhere
             if (k == 1) tile_dense<1, true>(smem, T, g, d.mats);
             else tile_dense<2, true>(smem, T, g, d.mats);
@@ -874,8 +950,8 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     const int tc_min_bits = tmb ? atoi(tmb) : 22;
     const bool use_tc = bs_tc_enabled() && !c64 && T == 12 && L == 5 && n_bits >= tc_min_bits;
     // fusion per sweep (independent, so on a few host threads); a sweep left with unfused 3/4-target
-    // gates keeps its plain gate list, since the tensor-core sweep kernel carries float-float paths for
-    // 1- and 2-target gates only
+    // gates or with reference-mode channels keeps its plain gate list, since the tensor-core sweep
+    // kernel carries float-float paths for 1- and 2-target gates only
     std::vector<std::vector<HostGate>> fused_all(use_tc ? sweeps.size() : 0);
     std::vector<char> fused_ok(fused_all.size(), 0);
     if (use_tc) {
@@ -889,7 +965,8 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
                 for (size_t q = 0; q < sw.hi_bits.size(); q++) local[sw.hi_bits[q]] = L + (int)q;
                 bs_fuse_tc(sw.gates, local, T, fused_all[i]);
                 bool ok = true;
-                for (const HostGate& hg : fused_all[i]) if (hg.kind != 1 && hg.kind != 4 && hg.k >= 3) ok = false;
+                for (const HostGate& hg : fused_all[i])
+                    if ((hg.kind != 1 && hg.kind != 4 && hg.k >= 3) || hg.kind == 5) ok = false;
                 fused_ok[i] = ok;
             }
         };
@@ -919,6 +996,29 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         for (size_t i = 0; i < sw.hi_bits.size(); i++) local[sw.hi_bits[i]] = L + (int)i;
         const std::vector<HostGate>* glist = (use_tc && fused_ok[si]) ? &fused_all[si] : &sw.gates;
         for (const HostGate& hg : *glist) {
+            if (hg.kind == 5) {
+                // reference-rule channel: its row and column target bits are tile bits (the planner needs them)
+                TileGate t{};
+                t.kind = 5;
+                t.k = hg.k;
+                const int nq = n_bits / 2, D = 1 << hg.k;
+                uint64_t rt = 0;
+                for (int q = 0; q < 2 * hg.k; q++) t.tbit[q] = local[hg.ebit[q]];
+                for (int q = 0; q < hg.k; q++) rt |= 1ULL << hg.ebit[q];
+                const uint64_t nt = (((uint64_t)1 << nq) - 1) & ~rt;
+                uint64_t unif = 0;
+                for (int b = 0; b < nq; b++)
+                    if (((nt >> b) & 1ULL) && local[b] < 0 && local[b + nq] < 0) unif |= 1ULL << b;
+                t.pmask[0] = nt;
+                t.pmask[1] = unif;
+                t.npar = (int32_t)(hg.mat.size() / (size_t)(2 * D * D));
+                t.mat_off = (int32_t)mats.size();
+                for (size_t e = 0; e + 1 < hg.mat.size(); e += 2) mats.push_back(to_cff(hg.mat[e], hg.mat[e + 1]));
+                ln.kmax = std::max(ln.kmax, 2 * hg.k);
+                tg.push_back(t);
+                ln.n_gates++;
+                continue;
+            }
             if (hg.kind == 4) {
                 TileGate t{};
                 t.kind = 4;
