@@ -23,6 +23,8 @@
 namespace {
 
 constexpr int kBlk = 4096;        // probabilities per CDF block
+constexpr int kChunk = 32;        // probabilities per chunk (one warp step of a search)
+constexpr int kCpb = kBlk / kChunk;   // chunks per block
 
 // mode bit 0: density matrix (diagonal of the stored matrix); bit 1: complex64 storage
 __device__ __forceinline__ double prob_at(const double2* st, int mode, int64_t dim, int64_t i) {
@@ -37,33 +39,63 @@ __device__ __forceinline__ double prob_at(const double2* st, int mode, int64_t d
     return ff2d(r.h, r.l);
 }
 
-__global__ void k_block_sums(const double2* __restrict__ st, int dm, int64_t dim, double* __restrict__ bsum) {
-    const int64_t b = blockIdx.x;
-    ffsum acc{0.f, 0.f};
-    for (int64_t i = b * kBlk + threadIdx.x; i < std::min<int64_t>(dim, (b + 1) * kBlk); i += blockDim.x) {
-        double p = prob_at(st, dm, dim, i);
-        ff f = d2ff(p);
-        fsum_add(acc, f.h, f.l);
+__device__ __forceinline__ void ff_warp_sum(ffsum& a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h = __shfl_xor_sync(0xffffffffu, a.h, o), l = __shfl_xor_sync(0xffffffffu, a.l, o);
+        fsum_add(a, h, l);
     }
-    // block reduce in float-float
-    __shared__ float sh[256], sl[256];
-    sh[threadIdx.x] = acc.h;
-    sl[threadIdx.x] = acc.l;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) {
-            ffsum a{sh[threadIdx.x], sl[threadIdx.x]};
-            fsum_add(a, sh[threadIdx.x + o], sl[threadIdx.x + o]);
-            sh[threadIdx.x] = a.h;
-            sl[threadIdx.x] = a.l;
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) bsum[b] = ff2d(sh[0], sl[0]);
 }
 
-// inclusive prefix of the block sums, one CTA (nb is at most 2^22)
-__global__ void k_scan_blocks(const double* __restrict__ bsum, int64_t nb, double* __restrict__ incl) {
+// Per block of kBlk probabilities: its float-float sum (bsum) and the inclusive prefix sums of its
+// kCpb chunks relative to the block start (cinc[b * kCpb + c]).  128 threads; warp w sums chunks
+// w, w + 4, ... with coalesced reads, warp 0 scans the chunk sums.
+__global__ void __launch_bounds__(128) k_block_sums(const double2* __restrict__ st, int dm, int64_t dim,
+                                                    double* __restrict__ bsum, double* __restrict__ cinc) {
+    __shared__ float ch[kCpb], cl[kCpb];
+    const int64_t b = blockIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int c = warp; c < kCpb; c += 4) {
+        const int64_t i = b * kBlk + (int64_t)c * kChunk + lane;
+        ffsum a{0.f, 0.f};
+        if (i < dim) {
+            const ff f = d2ff(prob_at(st, dm, dim, i));
+            a.h = f.h;
+            a.l = f.l;
+        }
+        ff_warp_sum(a);
+        if (lane == 0) { ch[c] = a.h; cl[c] = a.l; }
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    // lane holds chunks 4 lane .. 4 lane + 3: local inclusive sums, then a warp scan of the totals
+    ffsum loc[4];
+    ffsum run{0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        fsum_add(run, ch[4 * lane + k], cl[4 * lane + k]);
+        loc[k] = run;
+    }
+    ffsum pre = run;   // inclusive scan of the lane totals
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float h = __shfl_up_sync(0xffffffffu, pre.h, o), l = __shfl_up_sync(0xffffffffu, pre.l, o);
+        if (lane >= o) fsum_add(pre, h, l);
+    }
+    ffsum off{__shfl_up_sync(0xffffffffu, pre.h, 1), __shfl_up_sync(0xffffffffu, pre.l, 1)};
+    if (lane == 0) off = ffsum{0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        ffsum v = off;
+        fsum_add(v, loc[k].h, loc[k].l);
+        cinc[b * kCpb + 4 * lane + k] = ff2d(v.h, v.l);
+    }
+    if (lane == 31) bsum[b] = ff2d(pre.h, pre.l);
+}
+
+// inclusive prefix of the block sums, one CTA of 1024 threads (nb is at most 2^22): a serial sum
+// over each thread's run of blocks, then a parallel scan of the 1024 run totals
+__global__ void __launch_bounds__(1024) k_scan_blocks(const double* __restrict__ bsum, int64_t nb, double* __restrict__ incl) {
     __shared__ double part[1024];
     const int64_t per = (nb + blockDim.x - 1) / blockDim.x;
     const int64_t b0 = threadIdx.x * per, b1 = std::min<int64_t>(nb, b0 + per);
@@ -71,12 +103,13 @@ __global__ void k_scan_blocks(const double* __restrict__ bsum, int64_t nb, doubl
     for (int64_t b = b0; b < b1; b++) s += bsum[b];
     part[threadIdx.x] = s;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double run = 0.0;
-        for (int t = 0; t < (int)blockDim.x; t++) { double v = part[t]; part[t] = run; run += v; }
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        const double v = (int)threadIdx.x >= o ? part[threadIdx.x - o] : 0.0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
     }
-    __syncthreads();
-    double run = part[threadIdx.x];
+    double run = threadIdx.x ? part[threadIdx.x - 1] : 0.0;
     for (int64_t b = b0; b < b1; b++) { run += bsum[b]; incl[b] = run; }
 }
 
@@ -112,19 +145,28 @@ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
     return x ^ (x >> 31);
 }
 
-// The same search by a whole warp: block by binary search, then 32 probabilities per step with a
-// warp prefix sum and a ballot for the first running sum >= t (the prefix associates differently
-// from a left-to-right sum, so only exact boundary ties can land on a neighbouring index).
-__device__ int64_t cdf_find_warp(const double2* st, int dm, int64_t dim, const double* incl, int64_t nb, double t) {
+// The same search by a whole warp: block by binary search over the block prefix sums, chunk by
+// binary search over the block's chunk prefix sums, then 32 probabilities per step with a warp
+// prefix sum and a ballot for the first running sum >= t.  The sums associate differently from a
+// left-to-right scan, so only exact boundary ties can land on a neighbouring index.
+__device__ int64_t cdf_find_warp(const double2* st, int dm, int64_t dim, const double* incl, const double* cinc,
+                                 int64_t nb, double t) {
     const int lane = threadIdx.x & 31;
     int64_t lo = 0, hi = nb - 1;
     while (lo < hi) {
         const int64_t mid = (lo + hi) >> 1;
         if (incl[mid] >= t) hi = mid; else lo = mid + 1;
     }
-    double cw = (lo == 0) ? 0.0 : incl[lo - 1];
+    const double base = (lo == 0) ? 0.0 : incl[lo - 1];
+    const double* ci = cinc + lo * kCpb;
+    int clo = 0, chi = kCpb - 1;
+    while (clo < chi) {
+        const int mid = (clo + chi) >> 1;
+        if (base + ci[mid] >= t) chi = mid; else clo = mid + 1;
+    }
+    double cw = base + (clo == 0 ? 0.0 : ci[clo - 1]);
     const int64_t end = std::min<int64_t>(dim, (lo + 1) * kBlk);
-    for (int64_t c = lo * kBlk; c < end; c += 32) {
+    for (int64_t c = lo * kBlk + (int64_t)clo * kChunk; c < end; c += kChunk) {
         const int64_t i = c + lane;
         double p = (i < end) ? prob_at(st, dm, dim, i) : 0.0;
 #pragma unroll
@@ -141,12 +183,12 @@ __device__ int64_t cdf_find_warp(const double2* st, int dm, int64_t dim, const d
 
 // one shot per warp; uniforms from a counter-based splitmix64 stream
 __global__ void k_sample_rng(const double2* __restrict__ st, int dm, int64_t dim, const double* __restrict__ incl,
-                             int64_t nb, uint64_t seed, int64_t shots, int64_t* __restrict__ out) {
+                             const double* __restrict__ cinc, int64_t nb, uint64_t seed, int64_t shots, int64_t* __restrict__ out) {
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; s < shots; s += warps) {
         const uint64_t r = splitmix64(seed ^ splitmix64((uint64_t)s));
         const double u = (double)(r >> 11) * 0x1.0p-53;
-        const int64_t v = cdf_find_warp(st, dm, dim, incl, nb, u * incl[nb - 1]);
+        const int64_t v = cdf_find_warp(st, dm, dim, incl, cinc, nb, u * incl[nb - 1]);
         if ((threadIdx.x & 31) == 0) out[s] = v;
     }
 }
@@ -202,17 +244,23 @@ int grid(int64_t work, int threads) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((work + threads - 1) / threads, 152 * 8));
 }
 
-int build_cdf(bs_sim* s, double** incl_out, int64_t* nb_out) {
+// Scratch layout: bsum[nb] | incl[nb] | cinc[nb * kCpb] | extra_bytes for the caller (*extra).
+int build_cdf(bs_sim* s, double** incl_out, double** cinc_out, int64_t* nb_out, int64_t extra_bytes = 0,
+              void** extra = nullptr) {
     const int64_t dim = (int64_t)1 << s->n;
     const int64_t nb = (dim + kBlk - 1) / kBlk;
-    int rc = bs_ensure_scratch(s, 2 * nb * 8 + 1024);
+    const int64_t cdf_bytes = (2 * nb + nb * kCpb) * 8;
+    int rc = bs_ensure_scratch(s, cdf_bytes + extra_bytes + 64);
     if (rc) return rc;
     double* bsum = (double*)s->scratch;
     double* incl = bsum + nb;
-    k_block_sums<<<(unsigned)nb, 256, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, bsum);
+    double* cinc = incl + nb;
+    k_block_sums<<<(unsigned)nb, 128, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, bsum, cinc);
     k_scan_blocks<<<1, 1024, 0, s->stream>>>(bsum, nb, incl);
     *incl_out = incl;
+    if (cinc_out) *cinc_out = cinc;
     *nb_out = nb;
+    if (extra) *extra = (char*)s->scratch + ((cdf_bytes + 15) & ~(int64_t)15);
     return bs_cuda_check(s, cudaGetLastError(), "cdf");
 }
 
@@ -261,7 +309,7 @@ int bs_alias_build(bs_sim* s, double wsum, unsigned flags) {
         // sum of the weights in float-float on the device (block sums + scan)
         double* incl = nullptr;
         int64_t nb = 0;
-        rc = build_cdf(s, &incl, &nb);
+        rc = build_cdf(s, &incl, nullptr, &nb);
         if (rc) return rc;
         rc = bs_cuda_check(s, cudaMemcpyAsync(&wsum, incl + nb - 1, 8, cudaMemcpyDeviceToHost, s->stream), "weight sum");
         if (rc) return rc;
@@ -330,10 +378,8 @@ int bs_sample_direct(bs_sim* s, const double* u, int64_t shots, double wsum, int
     if (shots == 0) return BS_OK;
     double* incl = nullptr;
     int64_t nb = 0;
-    int rc = build_cdf(s, &incl, &nb);
-    if (rc) return rc;
     void* buf = nullptr;
-    rc = bs_cuda_check(s, cudaMallocAsync(&buf, (size_t)shots * 16, s->stream), "sample buffers");
+    int rc = build_cdf(s, &incl, nullptr, &nb, shots * 16, &buf);
     if (rc) return rc;
     double* du = (double*)buf;
     int64_t* dout = (int64_t*)(du + shots);
@@ -342,7 +388,6 @@ int bs_sample_direct(bs_sim* s, const double* u, int64_t shots, double wsum, int
     k_sample_direct<<<grid(shots, 128), 128, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, incl, nb,
                                                                du, wsum, shots, dout);
     cudaMemcpyAsync(out, dout, (size_t)shots * 8, cudaMemcpyDeviceToHost, s->stream);
-    cudaFreeAsync(buf, s->stream);
     return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "sample direct");
 }
 
@@ -351,18 +396,16 @@ int bs_sample(bs_sim* s, uint64_t seed, int64_t shots, int64_t* out) {
     if (shots < 0 || (shots > 0 && !out)) return bs_fail(s, BS_ERR_INVALID_ARG, "bad shot buffer");
     if (shots == 0) return BS_OK;
     double* incl = nullptr;
+    double* cinc = nullptr;
     int64_t nb = 0;
-    int rc = build_cdf(s, &incl, &nb);
-    if (rc) return rc;
     void* buf = nullptr;
-    rc = bs_cuda_check(s, cudaMallocAsync(&buf, (size_t)shots * 8, s->stream), "sample buffers");
+    int rc = build_cdf(s, &incl, &cinc, &nb, shots * 8, &buf);
     if (rc) return rc;
     int64_t* dout = (int64_t*)buf;
     const int64_t dim = (int64_t)1 << s->n;
-    k_sample_rng<<<grid(shots * 32, 128), 128, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, incl, nb,
+    k_sample_rng<<<grid(shots * 32, 128), 128, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, incl, cinc, nb,
                                                             seed, shots, dout);
     cudaMemcpyAsync(out, dout, (size_t)shots * 8, cudaMemcpyDeviceToHost, s->stream);
-    cudaFreeAsync(buf, s->stream);
     return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "sample");
 }
 

@@ -25,7 +25,7 @@
 //     (Re, Im) of digit j of amplitude t as a bf16 pair (low half = Re).
 // B (matrix digits): shared memory, K-major, no swizzle: 8x8 core matrices of
 //   128 B; per (digit i, k-step s) a 2 KiB block, row groups 256 B apart (SBO),
-//   the two K halves 128 B apart (LBO).  Built on the host by bs_tc_digits.
+//   the two K halves 128 B apart (LBO).  Made on the device by k_tc_digits.
 #pragma once
 #include <cstdint>
 
@@ -164,6 +164,61 @@ __device__ __forceinline__ float two_sum(float& s, float g) {
     return e;
 }
 
+// Two FP32 values in one aligned register pair (low half first), for the packed f32x2 instructions:
+// one issue slot per pair instead of two, the same rounding (round to nearest even) per half.
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 up(f2 v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// digits() on both halves
+__device__ __forceinline__ void digits2(f2 yh, f2 yl, f2 (&q)[6]) {
+    const f2 c0 = pk(12582912.0f, 12582912.0f), c1 = pk(49152.0f, 49152.0f), c2 = pk(192.0f, 192.0f),
+             c3 = pk(0.75f, 0.75f), c4 = pk(0.0029296875f, 0.0029296875f),
+             c5 = pk(1.1444091796875e-05f, 1.1444091796875e-05f);
+    f2 R = yh;
+    q[0] = sub2(add2(R, c0), c0);
+    R = sub2(R, q[0]);
+    q[1] = sub2(add2(R, c1), c1);
+    R = sub2(R, q[1]);
+    q[2] = sub2(add2(R, c2), c2);
+    R = add2(sub2(R, q[2]), yl);
+    q[3] = sub2(add2(R, c3), c3);
+    R = sub2(R, q[3]);
+    q[4] = sub2(add2(R, c4), c4);
+    R = sub2(R, q[4]);
+    q[5] = sub2(add2(R, c5), c5);
+}
+// two_sum() on both halves
+__device__ __forceinline__ f2 two_sum2(f2& s, f2 g) {
+    const f2 t = add2(s, g);
+    const f2 bb = sub2(t, s);
+    const f2 e = add2(sub2(s, sub2(t, bb)), sub2(g, bb));
+    s = t;
+    return e;
+}
+
 struct State {
     uint32_t tmem;             // TMEM base address
     uint32_t bar_u;            // digit-slice copy completion (1 arrival + bytes)
@@ -205,11 +260,13 @@ __device__ __forceinline__ void issue(const State& st, uint64_t b0, int round) {
     }
 }
 
-// Applies fused gate g to the (swizzled) 2^12 tile sm.  Called by all 256 threads of the CTA,
-// which then synchronise.  base: the CTA's global base index (selects the matrix variant).
+// Applies fused gate g to the (swizzled) 2^12 tile sm of float4 (re hi, im hi, re lo, im lo).
+// Called by all 256 threads of the CTA, which then synchronise.  base: the CTA's global base index
+// (selects the matrix variant).  s_tsw: 32 ints of shared scratch.  The swizzle is linear over
+// XOR, so the position of column m's amplitude t is sw(column bits) ^ sw(target bits of t).
 // On a wait that gives up, sets *fail and *err and leaves the tile partly updated.
 __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint16_t* __restrict__ pool, uint16_t* sB,
-                                      State& st, int64_t base, uint8_t* s_emax, int* s_tpos, int* s_fail, int* err) {
+                                      State& st, int64_t base, uint8_t* s_emax, int* s_tsw, int* s_fail, int* err) {
     const int tid = threadIdx.x, warp = tid >> 5, lane_id = tid & 31, m = tid & 127, h = tid >> 7;
     if (tid == 0) {
         // the previous readers of sB (the MMAs of the previous fused gate) have completed
@@ -227,38 +284,44 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
         int p = 0;
 #pragma unroll
         for (int q = 0; q < 5; q++) if ((tid >> q) & 1) p |= 1 << tb[q];
-        s_tpos[tid] = p;
+        s_tsw[tid] = sw(p);
     }
     int pm = 0;
     for (int b = 0, src = 0; b < 12; b++)
         if (!((tmask >> b) & 1u)) { pm |= ((m >> src) & 1) << b; src++; }
+    const int spm = sw(pm);
+    const int* tsw = s_tsw + 16 * h;
     __syncthreads();
     // column scale: largest exponent of the high words over the column (two threads per column)
-    uint32_t eb = 0;
+    {
+        const float2* hi = reinterpret_cast<const float2*>(sm);
+        uint32_t eb = 0;
 #pragma unroll 4
-    for (int a = 0; a < 16; a++) {
-        const float4 va = sm[sw(pm | s_tpos[16 * h + a])];
-        eb = max(eb, (__float_as_uint(va.x) >> 23) & 0xFFu);
-        eb = max(eb, (__float_as_uint(va.z) >> 23) & 0xFFu);
+        for (int a = 0; a < 16; a++) {
+            const float2 va = hi[2 * (spm ^ tsw[a])];
+            eb = max(eb, max(__float_as_uint(va.x) & 0x7F800000u, __float_as_uint(va.y) & 0x7F800000u));
+        }
+        s_emax[tid] = (uint8_t)(eb >> 23);
     }
-    s_emax[tid] = (uint8_t)eb;
     __syncthreads();
-    eb = max(eb, (uint32_t)s_emax[tid ^ 128]);
-    const int ebc = max((int)eb, max(6, 14 - g.tc_eu));
+    const int ebc = max((int)max(s_emax[tid], s_emax[tid ^ 128]), max(6, 14 - g.tc_eu));
     const float sc = __uint_as_float((uint32_t)(260 - ebc) << 23);                 // 2^(7 - E)
     const float osc = __uint_as_float((uint32_t)(ebc - 13 + g.tc_eu) << 23);       // 2^(E + eu - 14)
     const uint32_t lane = (uint32_t)((warp & 3) * 32) << 16;
+    const f2 sc2 = pk(sc, sc);
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         uint32_t w[6][4];
 #pragma unroll
         for (int a = 0; a < 4; a++) {
-            const float4 vv = sm[sw(pm | s_tpos[16 * h + 4 * c + a])];
-            float qr[6], qi[6];
-            digits(__fmul_rn(vv.x, sc), __fmul_rn(vv.y, sc), qr);
-            digits(__fmul_rn(vv.z, sc), __fmul_rn(vv.w, sc), qi);
+            const float4 vv = sm[spm ^ tsw[4 * c + a]];
+            f2 q[6];
+            digits2(mul2(pk(vv.x, vv.y), sc2), mul2(pk(vv.z, vv.w), sc2), q);
 #pragma unroll
-            for (int j = 0; j < 6; j++) w[j][a] = __byte_perm(__float_as_uint(qr[j]), __float_as_uint(qi[j]), 0x7632);
+            for (int j = 0; j < 6; j++) {
+                const float2 d = up(q[j]);
+                w[j][a] = __byte_perm(__float_as_uint(d.x), __float_as_uint(d.y), 0x7632);
+            }
         }
 #pragma unroll
         for (int j = 0; j < 6; j++) st4(st.tmem + lane + (uint32_t)(kA0 + 32 * j + 16 * h + 4 * c), w[j]);
@@ -276,9 +339,9 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
     __syncthreads();
     if (*s_fail) return;
     // Five rounds.  Every warp waits for the round's MMAs itself, folds the accumulator into its
-    // running float-float sums (the thread's 16 amplitudes x re/im) and arrives on bar_r; thread 0
-    // starts the next round once all eight warps have read the accumulator.
-    float s[32], e[32];
+    // running float-float sums (the thread's 16 amplitudes, re and im packed) and arrives on bar_r;
+    // thread 0 starts the next round once all eight warps have read the accumulator.
+    f2 S[16], E[16];
     bool ok = true;
 #pragma unroll 1
     for (int round = 0; round < 5; round++) {
@@ -294,12 +357,12 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
             ld8(st.tmem + lane + (uint32_t)(32 * h + 8 * c), r);
             wait_ld();
 #pragma unroll
-            for (int a = 0; a < 8; a++) {
-                const int o = 8 * c + a;
-                const float gv = __uint_as_float(r[a]);
-                if (round == 0) { s[o] = gv; e[o] = 0.f; }
-                else if (round <= 2) e[o] = __fadd_rn(e[o], two_sum(s[o], gv));
-                else e[o] = __fadd_rn(e[o], gv);
+            for (int p = 0; p < 4; p++) {
+                const int o = 4 * c + p;
+                const f2 gv = pk(__uint_as_float(r[2 * p]), __uint_as_float(r[2 * p + 1]));
+                if (round == 0) { S[o] = gv; E[o] = 0ull; }
+                else if (round <= 2) E[o] = add2(E[o], two_sum2(S[o], gv));
+                else E[o] = add2(E[o], gv);
             }
         }
         fence_before();
@@ -321,15 +384,13 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
         atomicExch(err, 1);
         return;
     }
+    const f2 osc2 = pk(osc, osc);
 #pragma unroll
     for (int a = 0; a < 16; a++) {
-        const int o = 2 * a;
-        float rh = __fadd_rn(s[o], e[o]);
-        float rl = __fsub_rn(e[o], __fsub_rn(rh, s[o]));
-        float ih = __fadd_rn(s[o + 1], e[o + 1]);
-        float il = __fsub_rn(e[o + 1], __fsub_rn(ih, s[o + 1]));
-        sm[sw(pm | s_tpos[16 * h + a])] = make_float4(__fmul_rn(rh, osc), __fmul_rn(rl, osc), __fmul_rn(ih, osc),
-                                                      __fmul_rn(il, osc));
+        const f2 hs = add2(S[a], E[a]);
+        const f2 ls = sub2(E[a], sub2(hs, S[a]));
+        const float2 hh = up(mul2(hs, osc2)), ll = up(mul2(ls, osc2));
+        sm[spm ^ tsw[a]] = make_float4(hh.x, hh.y, ll.x, ll.y);
     }
 }
 

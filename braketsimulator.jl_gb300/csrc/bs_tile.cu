@@ -27,8 +27,12 @@ __device__ __forceinline__ int insert0(int x, int bit) {
 // shared-memory index of tile element j: swizzled (tensor-core sweep) or plain
 template <bool SW>
 __device__ __forceinline__ int sx(int j) { return SW ? tc::sw(j) : j; }
-__device__ __forceinline__ cff f4c(float4 v) { return {v.x, v.y, v.z, v.w}; }
-__device__ __forceinline__ float4 c4f(const cff& c) { return make_float4(c.rh, c.rl, c.ih, c.il); }
+// Tile amplitudes in shared memory are float4 (re hi, im hi, re lo, im lo): the two high words and
+// the two low words each form an aligned register pair for the packed f32x2 arithmetic of the
+// tensor-core sweep.  Matrix entries in global memory are float4 (re hi, re lo, im hi, im lo).
+__device__ __forceinline__ cff f4c(float4 v) { return {v.x, v.z, v.y, v.w}; }
+__device__ __forceinline__ float4 c4f(const cff& c) { return make_float4(c.rh, c.ih, c.rl, c.il); }
+__device__ __forceinline__ cff f4m(float4 v) { return {v.x, v.y, v.z, v.w}; }
 
 template <int K, bool SW = false>
 __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* __restrict__ mats) {
@@ -50,7 +54,7 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
     for (int q = 0; q < K; q++) tb[q] = g.tbit[q];
     if (K == 1) {
         // 2x2: matrix held in registers across the thread's pairs
-        const cff m00 = f4c(__ldg(m)), m01 = f4c(__ldg(m + 1)), m10 = f4c(__ldg(m + 2)), m11 = f4c(__ldg(m + 3));
+        const cff m00 = f4m(__ldg(m)), m01 = f4m(__ldg(m + 1)), m10 = f4m(__ldg(m + 2)), m11 = f4m(__ldg(m + 3));
         const int b0 = 1 << tb[0];
 #pragma unroll 2
         for (int gr = threadIdx.x; gr < ngroups; gr += blockDim.x) {
@@ -87,9 +91,9 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
 #pragma unroll
         for (int r = 0; r < D; r++) {
             ffacc ar, ai;
-            cmac_first(ar, ai, f4c(__ldg(m + r * D)), x[0]);
+            cmac_first(ar, ai, f4m(__ldg(m + r * D)), x[0]);
 #pragma unroll
-            for (int c = 1; c < D; c++) cmac(ar, ai, f4c(__ldg(m + r * D + c)), x[c]);
+            for (int c = 1; c < D; c++) cmac(ar, ai, f4m(__ldg(m + r * D + c)), x[c]);
             sm[idx[r]] = c4f(cdone(ar, ai));
         }
     }
@@ -159,7 +163,7 @@ __device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const flo
             if (d.x == 0.f && d.z == 1.f) { sm[js] = c4f(cmul_ipow(f4c(sm[js]), 1)); continue; }
             if (d.x == 0.f && d.z == -1.f) { sm[js] = c4f(cmul_ipow(f4c(sm[js]), 3)); continue; }
         }
-        sm[js] = c4f(cmul(f4c(d), f4c(sm[js])));
+        sm[js] = c4f(cmul(f4m(d), f4c(sm[js])));
     }
 }
 
@@ -220,9 +224,9 @@ __device__ void tile_kraus_ref(float4* sm, int T, int L, const TileGate& g, cons
 #pragma unroll
                     for (int c = 0; c < D; c++) {
                         ffacc tr, ti;
-                        cmac_first(tr, ti, f4c(__ldg(Kq + i * D)), rho[0][c]);
+                        cmac_first(tr, ti, f4m(__ldg(Kq + i * D)), rho[0][c]);
 #pragma unroll
-                        for (int r = 1; r < D; r++) cmac(tr, ti, f4c(__ldg(Kq + i * D + r)), rho[r][c]);
+                        for (int r = 1; r < D; r++) cmac(tr, ti, f4m(__ldg(Kq + i * D + r)), rho[r][c]);
                         const cff t = cdone(tr, ti);
                         const float4 kj = __ldg(Kq + j * D + c);
                         const cff kc = {kj.x, kj.y, -kj.z, -kj.w};
@@ -316,7 +320,7 @@ __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ 
     __shared__ uint32_t s_tmem;
     __shared__ int64_t s_base;
     __shared__ int s_fail;
-    __shared__ int s_tpos[32];
+    __shared__ int s_tsw[32];
     __shared__ uint8_t s_emax[256];
     constexpr int T = 12, L = 5, H = 7, nt = 1 << T, lowmask = (1 << L) - 1;
     const int64_t tile = tile0 + (int64_t)blockIdx.x;
@@ -368,7 +372,7 @@ __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ 
                 st.tmem = s_tmem;
                 have = true;
             }
-            tc::apply(smem, g, d.tc_pool, sB, st, base, s_emax, s_tpos, &s_fail, d.err);
+            tc::apply(smem, g, d.tc_pool, sB, st, base, s_emax, s_tsw, &s_fail, d.err);
             if (gi == tc_last) {
                 __syncthreads();
                 if (warp == 0) tc::tmem_dealloc(st.tmem);
@@ -480,8 +484,8 @@ __global__ void __launch_bounds__(kThreads) k_dense_big(double2* __restrict__ ps
     float4* outv = smem + D;
     for (int r = threadIdx.x; r < D; r += blockDim.x) {
         ffacc ar, ai;
-        cmac_first(ar, ai, f4c(mat[(int64_t)r * D]), f4c(smem[0]));
-        for (int c = 1; c < D; c++) cmac(ar, ai, f4c(mat[(int64_t)r * D + c]), f4c(smem[c]));
+        cmac_first(ar, ai, f4m(mat[(int64_t)r * D]), f4c(smem[0]));
+        for (int c = 1; c < D; c++) cmac(ar, ai, f4m(mat[(int64_t)r * D + c]), f4c(smem[c]));
         outv[r] = c4f(cdone(ar, ai));
     }
     __syncthreads();
@@ -775,7 +779,7 @@ __device__ __forceinline__ void rb_diag(cff (&a)[16], int jt, const int (&rbm)[4
             if (d.x == 0.f && d.z == 1.f) { a[r] = cmul_ipow(a[r], 1); continue; }
             if (d.x == 0.f && d.z == -1.f) { a[r] = cmul_ipow(a[r], 3); continue; }
         }
-        a[r] = cmul(f4c(d), a[r]);
+        a[r] = cmul(f4m(d), a[r]);
     }
 }
 
@@ -847,7 +851,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_tile_rb(double2* __restrict_
             const int slot = (tpos == sg.reg[0]) ? 0 : (tpos == sg.reg[1]) ? 1 : (tpos == sg.reg[2]) ? 2 : 3;
             if (g.kind == 0) {
                 const float4* m = d.mats + g.mat_off;
-                const cff m00 = f4c(__ldg(m)), m01 = f4c(__ldg(m + 1)), m10 = f4c(__ldg(m + 2)), m11 = f4c(__ldg(m + 3));
+                const cff m00 = f4m(__ldg(m)), m01 = f4m(__ldg(m + 1)), m10 = f4m(__ldg(m + 2)), m11 = f4m(__ldg(m + 3));
                 switch (slot) {
                     case 0: rb_dense1<0>(a, jt, rbm, g.lc_mask, g.lc_val, m00, m01, m10, m11); break;
                     case 1: rb_dense1<1>(a, jt, rbm, g.lc_mask, g.lc_val, m00, m01, m10, m11); break;

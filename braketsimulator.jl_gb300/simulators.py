@@ -16,7 +16,7 @@ from typing import Sequence
 import numpy as np
 
 from . import _abi
-from .gates import Barrier, Delay, Gate, Measure, Reset, lower_gate
+from .gates import Barrier, Control, Delay, Gate, Measure, Reset, Unitary, lower_gate
 from .noises import Noise, lower_noise
 from .observables import (H, HermitianObservable, I, Observable, StandardObservable, TensorProduct, X, Y, Z,
                           diagonalizing_gates)
@@ -65,25 +65,49 @@ def _ops_for(instructions, dm: bool, noise_mode: int):
             continue
         if not isinstance(op, Gate):
             raise TypeError(f"cannot apply {op!r}")
-        for lg in lower_gate(op, t):
-            buf = _abi.cplx_buffer(lg.matrix)
+        for o, buf in _gate_ops(op, t):
             keep.append(buf)
-            o = _abi.BsOp()
-            o.kind = 0
-            o.flags = lg.flags | (_abi.BS_GATE_DIAGONAL if lg.diagonal else 0)
-            if len(lg.targets) > _abi.BS_MAX_TARGETS or len(lg.controls) > _abi.BS_MAX_CONTROLS:
-                raise ValueError("too many qubits in one instruction")
-            o.n_targets = len(lg.targets)
-            for j, q in enumerate(lg.targets):
-                o.targets[j] = q
-            o.n_controls = len(lg.controls)
-            for j, (q, v) in enumerate(zip(lg.controls, lg.control_values)):
-                o.controls[j] = q
-                o.control_values[j] = v
-            o.matrix = _abi.dptr(buf)
             ops.append(o)
     arr = (_abi.BsOp * max(1, len(ops)))(*ops)
     return arr, len(ops), keep
+
+
+# Lowered engine ops of fixed gates, keyed by (gate type, angles, pow_exponent, targets).  Gates
+# that carry a matrix or a sub-gate (Unitary, Control) are lowered every time.  The cached matrix
+# buffers are only read by the engine.
+_LOWER_CACHE: dict = {}
+_LOWER_CACHE_MAX = 1 << 16
+
+
+def _gate_ops(op, t):
+    key = None
+    if not isinstance(op, (Unitary, Control)):
+        key = (type(op), op.angle, op.pow_exponent, tuple(int(q) for q in t))
+        hit = _LOWER_CACHE.get(key)
+        if hit is not None:
+            return hit
+    res = []
+    for lg in lower_gate(op, t):
+        buf = _abi.cplx_buffer(lg.matrix)
+        o = _abi.BsOp()
+        o.kind = 0
+        o.flags = lg.flags | (_abi.BS_GATE_DIAGONAL if lg.diagonal else 0)
+        if len(lg.targets) > _abi.BS_MAX_TARGETS or len(lg.controls) > _abi.BS_MAX_CONTROLS:
+            raise ValueError("too many qubits in one instruction")
+        o.n_targets = len(lg.targets)
+        for j, q in enumerate(lg.targets):
+            o.targets[j] = q
+        o.n_controls = len(lg.controls)
+        for j, (q, v) in enumerate(zip(lg.controls, lg.control_values)):
+            o.controls[j] = q
+            o.control_values[j] = v
+        o.matrix = _abi.dptr(buf)
+        res.append((o, buf))
+    if key is not None:
+        if len(_LOWER_CACHE) >= _LOWER_CACHE_MAX:
+            _LOWER_CACHE.clear()
+        _LOWER_CACHE[key] = res
+    return res
 
 
 PRECISIONS = {"c128": _abi.BS_PREC_C128, "c64": _abi.BS_PREC_C64}
