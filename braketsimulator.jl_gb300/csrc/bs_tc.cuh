@@ -15,12 +15,14 @@
 // power of two and every partial sum below 2^24 of it, so these FP32 sums are
 // exact) and i+j = 4, 5, 6 together (rounding at 2^-56 of the result).  After
 // each round the CUDA cores fold the FP32 accumulator into a running
-// float-float sum.  What remains is the 48-bit truncation of both operands,
+// float-float sum, while the tensor cores run the next round into the other
+// of two accumulators.  What remains is the 48-bit truncation of both operands,
 // ~2^-46 of the column's largest value per fused gate.
 //
 // TMEM (256 columns per CTA, so that two CTAs share an SM and one's MMAs
 // overlap the other's CUDA-core work):
-//   D (one FP32 accumulator, reused by the five rounds): columns 0..63, lane m.
+//   D0, D1 (FP32 accumulators, lane m): columns 0..63, and columns 192..255 once
+//     round 4, the only reader of A digit slices 4 and 5, has completed.
 //   A (state digits): lanes 0..127 = columns m, TMEM columns kA0 + 32 j + t hold
 //     (Re, Im) of digit j of amplitude t as a bf16 pair (low half = Re).
 // B (matrix digits): shared memory, K-major, no swizzle: 8x8 core matrices of
@@ -119,6 +121,9 @@ __device__ __forceinline__ void st4(uint32_t taddr, const uint32_t (&w)[4]) {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "r"(w[0]), "r"(w[1]),
                  "r"(w[2]), "r"(w[3])
                  : "memory");
+}
+__device__ __forceinline__ void st2(uint32_t taddr, uint32_t w0, uint32_t w1) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1,%2};" ::"r"(taddr), "r"(w0), "r"(w1) : "memory");
 }
 __device__ __forceinline__ void ld8(uint32_t taddr, uint32_t (&r)[8]) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -220,21 +225,27 @@ __device__ __forceinline__ f2 two_sum2(f2& s, f2 g) {
 }
 
 struct State {
-    uint32_t tmem;             // TMEM base address
-    uint32_t bar_u;            // digit-slice copy completion (1 arrival + bytes)
-    uint32_t bar_m;            // MMA completion (commit)
-    uint32_t bar_r;            // accumulator read by every warp (8 arrivals)
-    uint32_t ph_u, ph_m, ph_r; // expected phase parities
+    uint32_t tmem;   // TMEM base address
+    uint32_t bar;    // five mbarriers 8 bytes apart: digit-slice copy (1 arrival + bytes), MMAs done into
+                     // D0, into D1 (commits), D0 read, D1 read (one arrival per warp)
+    uint32_t ph;     // expected phase parity of barrier k in bit k
 };
 
-// Thread 0: issue the MMAs of one digit-weight round into D, then commit to bar_m.  The round is a
-// compile-time constant so that the loops unroll and every operand address is the base plus a
-// constant: a single thread issues back to back (a run-time loop here doubled the time per MMA).
-// b0 = descriptor of the first digit slice; slice (i, s) starts (i*4+s)*2048 bytes later, which adds
-// (i*4+s)*128 to the 14-bit start-address field without carry (the slices span 48 KiB).
+constexpr uint32_t kD1 = kA0 + 128;   // second accumulator: the columns of A digit slices 4 and 5
+
+// Thread 0: issue the MMAs of one digit-weight round into the accumulator at TMEM column dcol,
+// then commit to bar.  The round is a compile-time constant so that the loops unroll and every
+// operand address is the base plus a constant: a single thread issues back to back (a run-time
+// loop here doubled the time per MMA).  b0 = descriptor of the first digit slice; slice (i, s)
+// starts (i*4+s)*2048 bytes later, which adds (i*4+s)*128 to the 14-bit start-address field
+// without carry (the slices span 48 KiB).
 template <int ROUND>
-__device__ __forceinline__ void issue_round(const State& st, uint64_t b0) {
+__device__ __forceinline__ void issue_round(uint32_t tmem, uint32_t dcol, uint64_t b0_, uint32_t bar) {
     constexpr int g0 = ROUND < 4 ? ROUND : 4, g1 = ROUND < 4 ? ROUND : 6;
+    // an opaque copy, so that the descriptors are formed here and not hoisted into registers
+    // held across the caller's loop
+    uint64_t b0;
+    asm volatile("mov.b64 %0, %1;" : "=l"(b0) : "l"(b0_));
     int n = 0;
 #pragma unroll
     for (int gs = g0; gs <= g1; gs++)
@@ -244,37 +255,41 @@ __device__ __forceinline__ void issue_round(const State& st, uint64_t b0) {
             for (int s = 0; s < 4; s++) {
                 const int i = gs - j;
                 if (i > 5 || j > 5) continue;
-                mma(st.tmem, st.tmem + (uint32_t)(kA0 + 32 * j + 8 * s), b0 + (uint64_t)((i * 4 + s) * 128),
+                mma(tmem + dcol, tmem + (uint32_t)(kA0 + 32 * j + 8 * s), b0 + (uint64_t)((i * 4 + s) * 128),
                     n == 0 ? 0u : 1u);
                 n++;
             }
-    commit(st.bar_m);
+    commit(bar);
 }
-__device__ __forceinline__ void issue(const State& st, uint64_t b0, int round) {
+__device__ __forceinline__ void issue(uint32_t tmem, uint32_t dcol, uint64_t b0, uint32_t bar, int round) {
     switch (round) {
-        case 0: issue_round<0>(st, b0); break;
-        case 1: issue_round<1>(st, b0); break;
-        case 2: issue_round<2>(st, b0); break;
-        case 3: issue_round<3>(st, b0); break;
-        default: issue_round<4>(st, b0); break;
+        case 0: issue_round<0>(tmem, dcol, b0, bar); break;
+        case 1: issue_round<1>(tmem, dcol, b0, bar); break;
+        case 2: issue_round<2>(tmem, dcol, b0, bar); break;
+        case 3: issue_round<3>(tmem, dcol, b0, bar); break;
+        default: issue_round<4>(tmem, dcol, b0, bar); break;
     }
 }
 
 // Applies fused gate g to the (swizzled) 2^12 tile sm of float4 (re hi, im hi, re lo, im lo).
-// Called by all 256 threads of the CTA, which then synchronise.  base: the CTA's global base index
-// (selects the matrix variant).  s_tsw: 32 ints of shared scratch.  The swizzle is linear over
-// XOR, so the position of column m's amplitude t is sw(column bits) ^ sw(target bits of t).
+// Called by all NT threads of the CTA (NT/128 threads per tile column, 32*128/NT amplitudes each),
+// which then synchronise.  base: the CTA's global base index (selects the matrix variant).  s_tsw:
+// 32 ints, s_emax: NT bytes of shared scratch.  The swizzle is linear over XOR, so the position of
+// column m's amplitude t is sw(column bits) ^ sw(target bits of t).
 // On a wait that gives up, sets *fail and *err and leaves the tile partly updated.
+template <int NT>
 __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint16_t* __restrict__ pool, uint16_t* sB,
                                       State& st, int64_t base, uint8_t* s_emax, int* s_tsw, int* s_fail, int* err) {
+    constexpr int HP = NT / 128;   // threads per column
+    constexpr int NA = 32 / HP;    // amplitudes per thread
     const int tid = threadIdx.x, warp = tid >> 5, lane_id = tid & 31, m = tid & 127, h = tid >> 7;
     if (tid == 0) {
         // the previous readers of sB (the MMAs of the previous fused gate) have completed
         int var = 0;
         for (int i = 0; i < g.tc_nu; i++) var |= (int)((base >> g.tc_ub[i]) & 1) << i;
-        mbar_expect_tx(st.bar_u, (uint32_t)kPoolBlock * 2);
+        mbar_expect_tx(st.bar, (uint32_t)kPoolBlock * 2);
         const uint16_t* src = pool + (size_t)(g.tc_off + var) * kPoolBlock;
-        for (int i = 0; i < 6; i++) bulk_g2s(su32(sB) + (uint32_t)i * 8192u, src + i * 4096, 8192u, st.bar_u);
+        for (int i = 0; i < 6; i++) bulk_g2s(su32(sB) + (uint32_t)i * 8192u, src + i * 4096, 8192u, st.bar);
     }
     int tb[5];
     uint32_t tmask = 0;
@@ -290,31 +305,34 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
     for (int b = 0, src = 0; b < 12; b++)
         if (!((tmask >> b) & 1u)) { pm |= ((m >> src) & 1) << b; src++; }
     const int spm = sw(pm);
-    const int* tsw = s_tsw + 16 * h;
+    const int* tsw = s_tsw + NA * h;
     __syncthreads();
-    // column scale: largest exponent of the high words over the column (two threads per column)
+    // column scale: largest exponent of the high words over the column (HP threads per column)
     {
         const float2* hi = reinterpret_cast<const float2*>(sm);
         uint32_t eb = 0;
 #pragma unroll 4
-        for (int a = 0; a < 16; a++) {
+        for (int a = 0; a < NA; a++) {
             const float2 va = hi[2 * (spm ^ tsw[a])];
             eb = max(eb, max(__float_as_uint(va.x) & 0x7F800000u, __float_as_uint(va.y) & 0x7F800000u));
         }
         s_emax[tid] = (uint8_t)(eb >> 23);
     }
     __syncthreads();
-    const int ebc = max((int)max(s_emax[tid], s_emax[tid ^ 128]), max(6, 14 - g.tc_eu));
+    int emax = s_emax[m];
+#pragma unroll
+    for (int k = 1; k < HP; k++) emax = max(emax, (int)s_emax[m + 128 * k]);
+    const int ebc = max(emax, max(6, 14 - g.tc_eu));
     const float sc = __uint_as_float((uint32_t)(260 - ebc) << 23);                 // 2^(7 - E)
     const float osc = __uint_as_float((uint32_t)(ebc - 13 + g.tc_eu) << 23);       // 2^(E + eu - 14)
     const uint32_t lane = (uint32_t)((warp & 3) * 32) << 16;
     const f2 sc2 = pk(sc, sc);
 #pragma unroll
-    for (int c = 0; c < 4; c++) {
-        uint32_t w[6][4];
+    for (int c = 0; c < NA / 2; c++) {
+        uint32_t w[6][2];
 #pragma unroll
-        for (int a = 0; a < 4; a++) {
-            const float4 vv = sm[spm ^ tsw[4 * c + a]];
+        for (int a = 0; a < 2; a++) {
+            const float4 vv = sm[spm ^ tsw[2 * c + a]];
             f2 q[6];
             digits2(mul2(pk(vv.x, vv.y), sc2), mul2(pk(vv.z, vv.w), sc2), q);
 #pragma unroll
@@ -324,7 +342,7 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
             }
         }
 #pragma unroll
-        for (int j = 0; j < 6; j++) st4(st.tmem + lane + (uint32_t)(kA0 + 32 * j + 16 * h + 4 * c), w[j]);
+        for (int j = 0; j < 6; j++) st2(st.tmem + lane + (uint32_t)(kA0 + 32 * j + NA * h + 2 * c), w[j][0], w[j][1]);
     }
     wait_st();
     fence_before();
@@ -332,51 +350,60 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
     fence_after();
     const uint64_t b0 = bdesc(su32(sB));
     if (tid == 0) {
-        if (mbar_wait(st.bar_u, st.ph_u)) issue_round<0>(st, b0);
+        if (mbar_wait(st.bar, st.ph & 1u)) issue_round<4>(st.tmem, 0u, b0, st.bar + 8u);
         else { *s_fail = 1; atomicExch(err, 1); }
     }
-    st.ph_u ^= 1u;
+    st.ph ^= 1u;
     __syncthreads();
     if (*s_fail) return;
-    // Five rounds.  Every warp waits for the round's MMAs itself, folds the accumulator into its
-    // running float-float sums (the thread's 16 amplitudes, re and im packed) and arrives on bar_r;
-    // thread 0 starts the next round once all eight warps have read the accumulator.
-    f2 S[16], E[16];
+    // The rounds run in the order 4, 3, 2, 1, 0 (smallest digit weights first) into two
+    // accumulators: D0 (columns 0..63) takes rounds 4, 2 and 0; D1 takes rounds 3 and 1, in the
+    // columns of A digit slices 4 and 5, which only round 4 reads.  Round 3 is issued as soon as
+    // round 4 has completed; every later round as soon as all warps have read the accumulator it
+    // reuses, so that the MMAs of one round run while the warps fold the previous one into their
+    // float-float sums (the thread's amplitudes, re and im packed).
+    f2 S[NA], E[NA];
     bool ok = true;
-#pragma unroll 1
-    for (int round = 0; round < 5; round++) {
+#pragma unroll
+    for (int k = 0; k < 5; k++) {   // unrolled: each step's fold and issue are then fixed code (a run-time k spilled)
+        const int acc = k & 1;
+        const uint32_t dcol = acc ? kD1 : 0u;
+        const uint32_t bm = st.bar + 8u * (1 + acc), br = st.bar + 8u * (3 + acc);
+        const uint32_t mbit = 2u << acc, rbit = 8u << acc;
         uint32_t done = 1;
-        if (lane_id == 0) done = mbar_wait(st.bar_m, st.ph_m) ? 1u : 0u;
+        if (lane_id == 0) done = mbar_wait(bm, (st.ph & mbit) ? 1u : 0u) ? 1u : 0u;
         done = __shfl_sync(0xffffffffu, done, 0);
-        st.ph_m ^= 1u;
+        st.ph ^= mbit;
         if (!done) { ok = false; break; }
         fence_after();
+        if (k == 0 && tid == 0) issue_round<3>(st.tmem, kD1, b0, st.bar + 16u);
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
+        for (int c = 0; c < NA / 4; c++) {
             uint32_t r[8];
-            ld8(st.tmem + lane + (uint32_t)(32 * h + 8 * c), r);
+            ld8(st.tmem + lane + dcol + (uint32_t)(2 * NA * h + 8 * c), r);
             wait_ld();
 #pragma unroll
             for (int p = 0; p < 4; p++) {
                 const int o = 4 * c + p;
                 const f2 gv = pk(__uint_as_float(r[2 * p]), __uint_as_float(r[2 * p + 1]));
-                if (round == 0) { S[o] = gv; E[o] = 0ull; }
-                else if (round <= 2) E[o] = add2(E[o], two_sum2(S[o], gv));
-                else E[o] = add2(E[o], gv);
+                if (k == 0) E[o] = gv;
+                else if (k == 1) E[o] = add2(E[o], gv);
+                else if (k == 2) S[o] = gv;
+                else E[o] = add2(E[o], two_sum2(S[o], gv));
             }
         }
         fence_before();
         __syncwarp();
-        if (lane_id == 0) mbar_arrive(st.bar_r);
-        if (round < 4 && tid == 0) {
-            if (mbar_wait(st.bar_r, st.ph_r)) {
+        if (lane_id == 0) mbar_arrive(br);
+        if (k + 2 <= 4 && tid == 0) {
+            if (mbar_wait(br, (st.ph & rbit) ? 1u : 0u)) {
                 fence_after();
-                issue(st, b0, round + 1);
+                issue(st.tmem, dcol, b0, bm, 2 - k);
             } else {
                 ok = false;
             }
         }
-        st.ph_r ^= 1u;
+        st.ph ^= rbit;
         if (!ok) break;
     }
     if (!ok) {
@@ -386,7 +413,7 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
     }
     const f2 osc2 = pk(osc, osc);
 #pragma unroll
-    for (int a = 0; a < 16; a++) {
+    for (int a = 0; a < NA; a++) {
         const f2 hs = add2(S[a], E[a]);
         const f2 ls = sub2(E[a], sub2(hs, S[a]));
         const float2 hh = up(mul2(hs, osc2)), ll = up(mul2(ls, osc2));

@@ -147,7 +147,7 @@ __device__ __forceinline__ bool parity_odd(const TileGate& g, int64_t gi) {
 // off_tab[h] << osh: global offset of the tile's high-bit pattern h
 template <typename OT, bool SW = false>
 __device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const float4* __restrict__ mats,
-                          int64_t base, const OT* off_tab, int osh) {
+                          int64_t base, OT off_tab, int osh) {
     const int nt = 1 << T, lowmask = (1 << L) - 1;
     const float4* m = mats + g.mat_off;
     for (int j = threadIdx.x; j < nt; j += blockDim.x) {
@@ -307,21 +307,34 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
 // two CTAs fit on an SM; each holds 256 of the SM's 512 TMEM columns (from its first to its last
 // fused gate), so one CTA's MMAs overlap the other's CUDA-core work.  The tile is stored with the
 // bank swizzle tc::sw.
-constexpr int kTcSmem = 49152 + 65536 + 512;
+#ifndef BS_TC_THREADS
+#define BS_TC_THREADS 256
+#endif
+constexpr int kTcThreads = BS_TC_THREADS;   // 256 (128 registers) or 512 (64 registers, spills; measured slower)
+constexpr int kTcSmem = 49152 + 65536;
 
-__global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ psi, SweepDesc d, int64_t tile0,
-                                                          int tc_last) {
+// Global offset (>> 5) of the tile's high-bit pattern i (7 bits) from two small tables:
+// a[i & 7] | b[i >> 3].
+struct HiOff {
+    const uint32_t* a;
+    const uint32_t* b;
+    __device__ __forceinline__ uint32_t operator[](int i) const { return a[i & 7] | b[i >> 3]; }
+};
+
+__global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __restrict__ psi, SweepDesc d, int64_t tile0,
+                                                                 int tc_last) {
     // 128-byte alignment: each 128-byte core matrix of the matrix operand sits in one shared-memory line
     extern __shared__ __align__(128) unsigned char dsm[];
     uint16_t* sB = reinterpret_cast<uint16_t*>(dsm);
     float4* smem = reinterpret_cast<float4*>(dsm + 49152);
-    uint32_t* off32 = reinterpret_cast<uint32_t*>(dsm + 49152 + 65536);   // global offset >> 5 per high pattern
-    __shared__ __align__(8) uint64_t bars[3];   // digit copy, MMA, accumulator read
+    __shared__ __align__(8) uint64_t bars[5];   // digit copy, MMAs into D0 / D1, D0 / D1 read
     __shared__ uint32_t s_tmem;
     __shared__ int64_t s_base;
     __shared__ int s_fail;
     __shared__ int s_tsw[32];
-    __shared__ uint8_t s_emax[256];
+    __shared__ uint32_t s_offa[8], s_offb[16];
+    __shared__ uint8_t s_emax[kTcThreads];
+    const HiOff off32{s_offa, s_offb};
     constexpr int T = 12, L = 5, H = 7, nt = 1 << T, lowmask = (1 << L) - 1;
     const int64_t tile = tile0 + (int64_t)blockIdx.x;
     if (threadIdx.x == 0) {
@@ -333,12 +346,16 @@ __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ 
         s_fail = 0;
         tc::mbar_init(tc::su32(&bars[0]));
         tc::mbar_init(tc::su32(&bars[1]));
-        tc::mbar_init_n(tc::su32(&bars[2]), 8);
+        tc::mbar_init(tc::su32(&bars[2]));
+        tc::mbar_init_n(tc::su32(&bars[3]), kTcThreads / 32);
+        tc::mbar_init_n(tc::su32(&bars[4]), kTcThreads / 32);
     }
-    for (int i = threadIdx.x; i < (1 << H); i += blockDim.x) {
+    if (threadIdx.x < 24) {
+        const int i = threadIdx.x < 8 ? threadIdx.x : (threadIdx.x - 8) << 3;
         int64_t o = 0;
         for (int j = 0; j < H; j++) if ((i >> j) & 1) o |= 1LL << d.hi_bits[j];
-        off32[i] = (uint32_t)(o >> L);
+        if (threadIdx.x < 8) s_offa[threadIdx.x] = (uint32_t)(o >> L);
+        else s_offb[threadIdx.x - 8] = (uint32_t)(o >> L);
     }
     __syncthreads();
     const int64_t base = s_base;
@@ -346,17 +363,18 @@ __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ 
     // tile load: each thread's 16 loads are issued together (coalesced 512 B rows), then converted to
     // float-float at the swizzled positions
     {
-        double2 x[16];
+        constexpr int NL = nt / kTcThreads;
+        double2 x[NL];
 #pragma unroll
-        for (int i = 0; i < 16; i++) {
-            const int j = i * 256 + (int)threadIdx.x;
+        for (int i = 0; i < NL; i++) {
+            const int j = i * kTcThreads + (int)threadIdx.x;
             x[i] = __ldcs(psi + (base | ((int64_t)off32[j >> L] << L) | (int64_t)(j & lowmask)));
         }
 #pragma unroll
-        for (int i = 0; i < 16; i++) smem[tc::sw(i * 256 + (int)threadIdx.x)] = c4f(load_c128(x[i]));
+        for (int i = 0; i < NL; i++) smem[tc::sw(i * kTcThreads + (int)threadIdx.x)] = c4f(load_c128(x[i]));
     }
     __syncthreads();
-    tc::State st{0u, tc::su32(&bars[0]), tc::su32(&bars[1]), tc::su32(&bars[2]), 0u, 0u, 0u};
+    tc::State st{0u, tc::su32(&bars[0]), 0u};
     bool have = false;
     for (int gi = 0; gi < d.n_gates; gi++) {
         const TileGate& g = d.gates[gi];
@@ -372,7 +390,7 @@ __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ 
                 st.tmem = s_tmem;
                 have = true;
             }
-            tc::apply(smem, g, d.tc_pool, sB, st, base, s_emax, s_tsw, &s_fail, d.err);
+            tc::apply<kTcThreads>(smem, g, d.tc_pool, sB, st, base, s_emax, s_tsw, &s_fail, d.err);
             if (gi == tc_last) {
                 __syncthreads();
                 if (warp == 0) tc::tmem_dealloc(st.tmem);
@@ -388,7 +406,7 @@ __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ 
                 }
             }
         } else if (kind == 1) {
-            tile_diag<uint32_t, true>(smem, T, L, g, d.mats, base, off32, L);
+            tile_diag<HiOff, true>(smem, T, L, g, d.mats, base, off32, L);
 
         } else if (kind == 0) {   // the planner routes sweeps with unfused 3- or 4-target gates elsewhere
             if (k == 1) tile_dense<1, true>(smem, T, g, d.mats);
@@ -402,16 +420,17 @@ __global__ void __launch_bounds__(256, 2) k_tile_sweep_tc(double2* __restrict__ 
     if (have) {
         // a wait gave up: give the copies and MMAs in flight a bounded time to land before releasing TMEM
         if (threadIdx.x == 0 && s_fail) {
-            tc::mbar_wait(st.bar_u, st.ph_u);
-            tc::mbar_wait(st.bar_m, st.ph_m);
+            tc::mbar_wait(st.bar, st.ph & 1u);
+            tc::mbar_wait(st.bar + 8u, (st.ph >> 1) & 1u);
+            tc::mbar_wait(st.bar + 16u, (st.ph >> 2) & 1u);
         }
         __syncthreads();
         if (warp == 0) tc::tmem_dealloc(st.tmem);
     }
     // tile store: streaming stores, nothing waits for them
 #pragma unroll 4
-    for (int i = 0; i < 16; i++) {
-        const int j = i * 256 + (int)threadIdx.x;
+    for (int i = 0; i < nt / kTcThreads; i++) {
+        const int j = i * kTcThreads + (int)threadIdx.x;
         __stcs(psi + (base | ((int64_t)off32[j >> L] << L) | (int64_t)(j & lowmask)), store_c128(f4c(smem[tc::sw(j)])));
     }
 }
@@ -1269,7 +1288,7 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
                     s->tc_events.push_back(e);
                 }
                 cudaEventRecord(s->tc_events[pe], s->stream);
-                k_tile_sweep_tc<<<(unsigned)nb, 256, kTcSmem, s->stream>>>(psi, d, t0, ln.tc_last);
+                k_tile_sweep_tc<<<(unsigned)nb, kTcThreads, kTcSmem, s->stream>>>(psi, d, t0, ln.tc_last);
                 cudaEventRecord(s->tc_events[pe + 1], s->stream);
                 s->tc_events_used++;
                 s->stats.tc_launches++;
