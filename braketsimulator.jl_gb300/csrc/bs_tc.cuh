@@ -6,9 +6,9 @@
 //     out[2t'+c'] = sum_k U_real[2t'+c'][k] x[k],  x[2t+0] = Re a_t, x[2t+1] = Im a_t
 // the gate is D[128 x 64] = A[128 x 64] * U_real^T, one tcgen05 GEMM per tile.
 //
-// Exactness (Ozaki-style split): every column is scaled by a power of two so
-// that |x| < 1, and both x (on the device) and U_real (on the host) are split
-// into six balanced 8-bit digits, digit j carried as bf16 d_j * 2^(-8j) with
+// Exactness (Ozaki-style split): the tile is scaled by a power of two (from the
+// largest exponent over the tile) so that |x| < 2^8, and both x and U_real (on
+// the device, from the FP64 matrix) are split into six balanced 8-bit digits, digit j carried as bf16 d_j * 2^(-8j) with
 // |d_j| <= 128 (256 for the one digit that absorbs the float-float low word).
 // The 26 digit pairs with i + j <= 6 are accumulated in five rounds by digit
 // weight: i+j = 0, 1, 2, 3 each alone (every product a multiple of the same
@@ -17,7 +17,7 @@
 // each round the CUDA cores fold the FP32 accumulator into a running
 // float-float sum, while the tensor cores run the next round into the other
 // of two accumulators.  What remains is the 48-bit truncation of both operands,
-// ~2^-46 of the column's largest value per fused gate.
+// ~2^-46 of the tile's largest value per fused gate.
 //
 // TMEM (256 columns per CTA, so that two CTAs share an SM and one's MMAs
 // overlap the other's CUDA-core work):
@@ -274,22 +274,26 @@ __device__ __forceinline__ void issue(uint32_t tmem, uint32_t dcol, uint64_t b0,
 // Applies fused gate g to the (swizzled) 2^12 tile sm of float4 (re hi, im hi, re lo, im lo).
 // Called by all NT threads of the CTA (NT/128 threads per tile column, 32*128/NT amplitudes each),
 // which then synchronise.  base: the CTA's global base index (selects the matrix variant).  s_tsw:
-// 32 ints, s_emax: NT bytes of shared scratch.  The swizzle is linear over XOR, so the position of
-// column m's amplitude t is sw(column bits) ^ sw(target bits of t).
+// 32 ints of shared scratch; s_wmax: NT/32 per-warp maxima of the high words' exponent fields.
+// The swizzle is linear over XOR, so the position of column m's amplitude t is
+// sw(column bits) ^ sw(target bits of t).
 // On a wait that gives up, sets *fail and *err and leaves the tile partly updated.
 template <int NT>
 __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint16_t* __restrict__ pool, uint16_t* sB,
-                                      State& st, int64_t base, uint8_t* s_emax, int* s_tsw, int* s_fail, int* err) {
+                                      State& st, int64_t base, uint32_t* s_wmax, bool emax_ok, int* s_tsw,
+                                      int* s_fail, int* err) {
     constexpr int HP = NT / 128;   // threads per column
     constexpr int NA = 32 / HP;    // amplitudes per thread
     const int tid = threadIdx.x, warp = tid >> 5, lane_id = tid & 31, m = tid & 127, h = tid >> 7;
-    if (tid == 0) {
-        // the previous readers of sB (the MMAs of the previous fused gate) have completed
+    if (tid < 6) {
+        // the previous readers of sB (the MMAs of the previous fused gate) have completed; lanes 0..5
+        // each copy one 8 KiB digit slice of the CTA's matrix variant
         int var = 0;
         for (int i = 0; i < g.tc_nu; i++) var |= (int)((base >> g.tc_ub[i]) & 1) << i;
-        mbar_expect_tx(st.bar, (uint32_t)kPoolBlock * 2);
+        if (tid == 0) mbar_expect_tx(st.bar, (uint32_t)kPoolBlock * 2);
+        __syncwarp(0x3fu);
         const uint16_t* src = pool + (size_t)(g.tc_off + var) * kPoolBlock;
-        for (int i = 0; i < 6; i++) bulk_g2s(su32(sB) + (uint32_t)i * 8192u, src + i * 4096, 8192u, st.bar);
+        bulk_g2s(su32(sB) + (uint32_t)tid * 8192u, src + tid * 4096, 8192u, st.bar);
     }
     int tb[5];
     uint32_t tmask = 0;
@@ -306,23 +310,25 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
         if (!((tmask >> b) & 1u)) { pm |= ((m >> src) & 1) << b; src++; }
     const int spm = sw(pm);
     const int* tsw = s_tsw + NA * h;
-    __syncthreads();
-    // column scale: largest exponent of the high words over the column (HP threads per column)
-    {
+    // Tile scale: the largest exponent of the high words over the tile, per warp in s_wmax.  It was
+    // left there by the previous fused gate's write-back or the tile load unless a gate that may
+    // change magnitudes ran since (emax_ok false); then it is taken here in one pass.
+    if (!emax_ok) {
         const float2* hi = reinterpret_cast<const float2*>(sm);
         uint32_t eb = 0;
 #pragma unroll 4
-        for (int a = 0; a < NA; a++) {
-            const float2 va = hi[2 * (spm ^ tsw[a])];
+        for (int a = 0; a < 4096 / NT; a++) {
+            const float2 va = hi[2 * (a * NT + tid)];
             eb = max(eb, max(__float_as_uint(va.x) & 0x7F800000u, __float_as_uint(va.y) & 0x7F800000u));
         }
-        s_emax[tid] = (uint8_t)(eb >> 23);
+        eb = __reduce_max_sync(0xffffffffu, eb);
+        if (lane_id == 0) s_wmax[warp] = eb;
     }
     __syncthreads();
-    int emax = s_emax[m];
+    uint32_t eall = s_wmax[0];
 #pragma unroll
-    for (int k = 1; k < HP; k++) emax = max(emax, (int)s_emax[m + 128 * k]);
-    const int ebc = max(emax, max(6, 14 - g.tc_eu));
+    for (int w = 1; w < NT / 32; w++) eall = max(eall, s_wmax[w]);
+    const int ebc = max((int)(eall >> 23), max(6, 14 - g.tc_eu));
     const float sc = __uint_as_float((uint32_t)(260 - ebc) << 23);                 // 2^(7 - E)
     const float osc = __uint_as_float((uint32_t)(ebc - 13 + g.tc_eu) << 23);       // 2^(E + eu - 14)
     const uint32_t lane = (uint32_t)((warp & 3) * 32) << 16;
@@ -412,13 +418,18 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
         return;
     }
     const f2 osc2 = pk(osc, osc);
+    uint32_t eb = 0;
 #pragma unroll
     for (int a = 0; a < NA; a++) {
         const f2 hs = add2(S[a], E[a]);
         const f2 ls = sub2(E[a], sub2(hs, S[a]));
         const float2 hh = up(mul2(hs, osc2)), ll = up(mul2(ls, osc2));
         sm[spm ^ tsw[a]] = make_float4(hh.x, hh.y, ll.x, ll.y);
+        eb = max(eb, max(__float_as_uint(hh.x) & 0x7F800000u, __float_as_uint(hh.y) & 0x7F800000u));
     }
+    // the next fused gate's tile scale (read after the caller's barrier)
+    eb = __reduce_max_sync(0xffffffffu, eb);
+    if (lane_id == 0) s_wmax[warp] = eb;
 }
 
 }  // namespace tc

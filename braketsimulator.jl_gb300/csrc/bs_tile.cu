@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
     __shared__ int s_fail;
     __shared__ int s_tsw[32];
     __shared__ uint32_t s_offa[8], s_offb[16];
-    __shared__ uint8_t s_emax[kTcThreads];
+    __shared__ uint32_t s_wmax[kTcThreads / 32];   // per-warp largest high-word exponent field
     const HiOff off32{s_offa, s_offb};
     constexpr int T = 12, L = 5, H = 7, nt = 1 << T, lowmask = (1 << L) - 1;
     const int64_t tile = tile0 + (int64_t)blockIdx.x;
@@ -370,16 +370,25 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
             const int j = i * kTcThreads + (int)threadIdx.x;
             x[i] = __ldcs(psi + (base | ((int64_t)off32[j >> L] << L) | (int64_t)(j & lowmask)));
         }
+        uint32_t eb = 0;
 #pragma unroll
-        for (int i = 0; i < NL; i++) smem[tc::sw(i * kTcThreads + (int)threadIdx.x)] = c4f(load_c128(x[i]));
+        for (int i = 0; i < NL; i++) {
+            const float4 v = c4f(load_c128(x[i]));
+            smem[tc::sw(i * kTcThreads + (int)threadIdx.x)] = v;
+            eb = max(eb, max(__float_as_uint(v.x) & 0x7F800000u, __float_as_uint(v.y) & 0x7F800000u));
+        }
+        eb = __reduce_max_sync(0xffffffffu, eb);
+        if ((threadIdx.x & 31) == 0) s_wmax[threadIdx.x >> 5] = eb;
     }
     __syncthreads();
     tc::State st{0u, tc::su32(&bars[0]), 0u};
     bool have = false;
+    bool emax_ok = true;   // s_wmax holds the tile's largest exponent (no magnitude-changing gate since)
     for (int gi = 0; gi < d.n_gates; gi++) {
         const TileGate& g = d.gates[gi];
         if ((base & (int64_t)g.gc_mask) != (int64_t)g.gc_val) continue;
         const int kind = g.kind, k = g.k;
+        if (kind == 0 || kind == 1) emax_ok = false;   // dense and diagonal gates may change magnitudes
         if (kind == 4) {
             if (s_fail) continue;
             if (!have) {
@@ -390,7 +399,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
                 st.tmem = s_tmem;
                 have = true;
             }
-            tc::apply<kTcThreads>(smem, g, d.tc_pool, sB, st, base, s_emax, s_tsw, &s_fail, d.err);
+            tc::apply<kTcThreads>(smem, g, d.tc_pool, sB, st, base, s_wmax, emax_ok, s_tsw, &s_fail, d.err);
+            emax_ok = true;
             if (gi == tc_last) {
                 __syncthreads();
                 if (warp == 0) tc::tmem_dealloc(st.tmem);
