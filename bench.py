@@ -342,11 +342,27 @@ def batch_bench(bs):
     e128, _, _ = bs.batch_simulate([circuits[c] for c in small], [counts[c] for c in small], [obs[c] for c in small],
                                    shots=0, precision="c128")
     err = float(np.max(np.abs(exp[small] - e128)))
+    # the same batch captured once into a CUDA graph, then replayed (host work per replay: one
+    # graph launch and the result copies)
+    t0 = time.perf_counter()
+    cb = bs.CapturedBatch(circuits, counts, obs, shots=1000, seed=2, precision="c64")
+    t_cap = time.perf_counter() - t0
+    cb.launch()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        exp2, _, st2 = cb.launch()
+    t_rep = (time.perf_counter() - t0) / reps
+    same = bool(np.array_equal(exp, exp2))
+    cb.close()
     return {"circuits": len(circuits), "qubits": "12..26", "gates": int(sum(len(c) for c in circuits)),
             "shots_each": 1000, "expectations_each": 8, "precision": "c64 (FP64 reductions)",
             "s_per_batch": round(dt, 3), "circuits_per_s": round(len(circuits) / dt, 1),
             "device_ms": round(st["gpu_ms"], 1), "sweeps": st["sweeps"],
-            "max_abs_err_c64_vs_c128_expectations": err}
+            "max_abs_err_c64_vs_c128_expectations": err,
+            "graph": {"capture_s": round(t_cap, 3), "s_per_replay": round(t_rep, 3),
+                      "circuits_per_s": round(len(circuits) / t_rep, 1), "device_ms": round(st2["gpu_ms"], 1),
+                      "replay_equals_one_shot": same}}
 
 
 def run_reference(args, rank, world):

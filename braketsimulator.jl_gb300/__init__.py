@@ -18,7 +18,7 @@ from .results import (Amplitude, DensityMatrix, Expectation, Probability, Sample
                       calculate, marginal_probability, partial_trace, permute_density_matrix, permute_probability)
 from .adjoint import adjoint_gradient, parameter_shift_gradient  # noqa: F401
 from .program import Program, simulate, create_sim  # noqa: F401
-from .batch import batch_simulate  # noqa: F401
+from .batch import CapturedBatch, batch_simulate  # noqa: F401
 
 
 def library_path() -> str:

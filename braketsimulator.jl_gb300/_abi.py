@@ -92,6 +92,11 @@ SIGNATURES = {
     "bs_expectation_pauli_noalloc": (_i32, [_p, _i32, _i32, _i32, _P(_u64), _P(_u64), _P(_f64), _P(_f64), _p]),
     "bs_run_batch": (_i32, [_i32, _P(_i32), _P(_P(BsOp)), _P(_i64), _i32, _P(_u64), _P(_u64), _i64, _u64, _i32,
                             _P(_f64), _P(_i64), _P(BsStats)]),
+    "bs_batch_create": (_i32, [_i32, _P(_i32), _P(_P(BsOp)), _P(_i64), _i32, _P(_u64), _P(_u64), _i64, _u64, _i32,
+                               _P(_p)]),
+    "bs_batch_set_ops": (_i32, [_p, _P(_P(BsOp)), _P(_i64)]),
+    "bs_batch_launch": (_i32, [_p, _P(_f64), _P(_i64), _P(BsStats)]),
+    "bs_batch_destroy": (_i32, [_p]),
     "bs_synchronize": (_i32, [_p]),
     "bs_state_device_ptr": (_i32, [_p, _P(_p)]),
 }

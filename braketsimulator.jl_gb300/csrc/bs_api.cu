@@ -15,8 +15,47 @@ int bs_cuda_check(bs_sim* s, cudaError_t e, const char* what) {
 }
 int bs_vec_bits(const bs_sim* s) { return s->kind == BS_KIND_DM ? 2 * s->n : s->n; }
 
+char* bs_stage(bs_sim* s, size_t bytes) {
+    bytes = (bytes + 255) & ~(size_t)255;
+    if (s->capturing) {
+        if (s->arena.empty() || s->arena_used + bytes > s->arena.back().second) {
+            const size_t cap = std::max(bytes, (size_t)4 << 20);
+            char* p = nullptr;
+            if (cudaMallocHost(&p, cap) != cudaSuccess) return nullptr;
+            s->arena.push_back({p, cap});
+            s->arena_used = 0;
+        }
+        char* p = s->arena.back().first + s->arena_used;
+        s->arena_used += bytes;
+        return p;
+    }
+    if (s->hstage_pending) {
+        cudaEventSynchronize(s->hstage_ev);
+        s->hstage_pending = false;
+    }
+    if (bytes > s->hstage_cap) {
+        if (s->hstage) cudaFreeHost(s->hstage);
+        s->hstage = nullptr;
+        s->hstage_cap = 0;
+        if (cudaMallocHost(&s->hstage, bytes) != cudaSuccess) return nullptr;
+        s->hstage_cap = bytes;
+    }
+    return s->hstage;
+}
+void bs_stage_done(bs_sim* s) {
+    if (s->capturing) return;
+    cudaEventRecord(s->hstage_ev, s->stream);
+    s->hstage_pending = true;
+}
+void bs_arena_release(bs_sim* s) {
+    for (auto& c : s->arena) cudaFreeHost(c.first);
+    s->arena.clear();
+    s->arena_used = 0;
+}
+
 int bs_ensure_scratch(bs_sim* s, int64_t bytes) {
     if (s->scratch_bytes >= bytes) return BS_OK;
+    if (s->capturing) return bs_fail(s, BS_ERR_STATE, "scratch growth during graph capture");
     if (s->scratch) cudaFree(s->scratch);
     s->scratch = nullptr;
     s->scratch_bytes = 0;
@@ -27,6 +66,7 @@ int bs_ensure_scratch(bs_sim* s, int64_t bytes) {
 }
 int bs_ensure_plan(bs_sim* s, int64_t bytes) {
     if (s->plan_bytes >= bytes) return BS_OK;
+    if (s->capturing) return bs_fail(s, BS_ERR_STATE, "plan buffer growth during graph capture");
     // the previous plan may still be read by queued kernels
     cudaStreamSynchronize(s->stream);
     if (s->plan_buf) cudaFree(s->plan_buf);
@@ -87,6 +127,7 @@ int alloc_state(bs_sim* s, int n) {
     const int64_t len = (int64_t)1 << bits;
     const int64_t bytes = len * elem_bytes(s);
     if (bytes > s->cap_bytes) {
+        if (s->capturing) return bs_fail(s, BS_ERR_STATE, "state growth during graph capture");
         if (s->state) cudaFree(s->state);
         s->state = nullptr;
         s->cap_bytes = 0;
@@ -125,6 +166,7 @@ int bs_create(int kind, int n_qubits, int precision, bs_sim** out) {
     int rc = bs_cuda_check(s, cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream");
     if (!rc) rc = bs_cuda_check(s, cudaEventCreate(&s->ev0), "event");
     if (!rc) rc = bs_cuda_check(s, cudaEventCreate(&s->ev1), "event");
+    if (!rc) rc = bs_cuda_check(s, cudaEventCreateWithFlags(&s->hstage_ev, cudaEventDisableTiming), "event");
     if (!rc) rc = alloc_state(s, n_qubits);
     if (rc) { bs_destroy(s); return rc; }
     *out = s;
@@ -143,6 +185,9 @@ int bs_destroy(bs_sim* s) {
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     for (cudaEvent_t e : s->tc_events) cudaEventDestroy(e);
+    if (s->hstage_ev) cudaEventDestroy(s->hstage_ev);
+    if (s->hstage) cudaFreeHost(s->hstage);
+    bs_arena_release(s);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return BS_OK;
@@ -269,7 +314,7 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     s->stats = bs_stats{};
     s->tc_events_used = 0;
     s->alias_valid = false;
-    cudaEventRecord(s->ev0, s->stream);
+    if (!s->capturing) cudaEventRecord(s->ev0, s->stream);
     std::vector<HostGate> pending;
     auto flush = [&]() -> int {
         if (pending.empty()) return BS_OK;
@@ -306,6 +351,7 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     }
     int rc = flush();
     if (rc) return rc;
+    if (s->capturing) return BS_OK;   // the graph's launcher synchronises and checks
     cudaEventRecord(s->ev1, s->stream);
     rc = bs_cuda_check(s, cudaEventSynchronize(s->ev1), "evolve");
     if (rc) return rc;

@@ -97,6 +97,17 @@ struct bs_sim {
     size_t tc_events_used = 0;            // pairs recorded since the last bs_collect_tc_time
     bs_stats stats{};
     std::string err;
+    // Host staging of uploads: pinned, reused once the previous upload has landed (hstage_ev).
+    char* hstage = nullptr;
+    size_t hstage_cap = 0;
+    cudaEvent_t hstage_ev = nullptr;
+    bool hstage_pending = false;
+    // While the handle's stream is captured into a CUDA graph: no host synchronisation, no device
+    // buffer growth, and staging comes from an append-only pinned arena that lives as long as the
+    // graph (the graph's copy nodes read it on every replay).
+    bool capturing = false;
+    std::vector<std::pair<char*, size_t>> arena;   // chunks (pointer, capacity)
+    size_t arena_used = 0;                          // bytes used in the last chunk
 };
 
 // ---- helpers implemented in bs_api.cu
@@ -104,6 +115,11 @@ int bs_fail(bs_sim* s, int code, const std::string& msg);
 int bs_cuda_check(bs_sim* s, cudaError_t e, const char* what);
 int bs_ensure_scratch(bs_sim* s, int64_t bytes);
 int bs_ensure_plan(bs_sim* s, int64_t bytes);
+// Pinned host region for one upload of `bytes`; call bs_stage_done after queuing the copy.
+char* bs_stage(bs_sim* s, size_t bytes);
+void bs_stage_done(bs_sim* s);
+// Release the capture arena (the graph that read it is gone).
+void bs_arena_release(bs_sim* s);
 int bs_vec_bits(const bs_sim* s);
 
 // ---- lowering (bs_plan.cpp)

@@ -310,6 +310,11 @@ int bs_expectation_pauli(bs_sim* s, int n_terms, const uint64_t* xmask, const ui
     k_sum_partials<<<n_terms, 256, 0, s->stream>>>(partial, nb, n_terms, res);
     rc = bs_cuda_check(s, cudaMemcpyAsync(out, res, (size_t)n_terms * 8, cudaMemcpyDeviceToHost, s->stream), "expectation");
     if (rc) return rc;
+    if (s->capturing) {
+        // out is the graph owner's pinned buffer, filled on every replay
+        if (coeffs) return bs_fail(s, BS_ERR_INVALID_ARG, "coefficients are applied after a captured graph runs");
+        return BS_OK;
+    }
     rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "expectation sync");
     if (rc) return rc;
     if (coeffs)

@@ -406,6 +406,7 @@ int bs_sample(bs_sim* s, uint64_t seed, int64_t shots, int64_t* out) {
     k_sample_rng<<<grid(shots * 32, 128), 128, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, incl, cinc, nb,
                                                             seed, shots, dout);
     cudaMemcpyAsync(out, dout, (size_t)shots * 8, cudaMemcpyDeviceToHost, s->stream);
+    if (s->capturing) return bs_cuda_check(s, cudaGetLastError(), "sample");   // out: the graph owner's pinned buffer
     return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "sample");
 }
 

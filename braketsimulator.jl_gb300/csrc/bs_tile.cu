@@ -1189,19 +1189,22 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     const int64_t o_tm = b_tg + b_m + b_p + b_s, o_ts = o_tm + b_tm, o_tc = o_ts + b_ts;
     int rc = bs_ensure_plan(s, o_tc + b_tc);
     if (rc) return rc;
-    std::vector<char> host((size_t)o_tc, 0);
+    char* host = bs_stage(s, (size_t)o_tc);
+    if (!host) return bs_fail(s, BS_ERR_ALLOC, "pinned staging allocation");
+    std::memset(host, 0, (size_t)o_tc);
     if (!tc_mats.empty()) {
-        std::memcpy(host.data() + o_tm, tc_mats.data(), tc_mats.size() * sizeof(double));
-        std::memcpy(host.data() + o_ts, tc_scale.data(), tc_scale.size() * sizeof(double));
+        std::memcpy(host + o_tm, tc_mats.data(), tc_mats.size() * sizeof(double));
+        std::memcpy(host + o_ts, tc_scale.data(), tc_scale.size() * sizeof(double));
     }
-    if (!segs.empty()) std::memcpy(host.data() + b_tg + b_m + b_p, segs.data(), segs.size() * sizeof(RBSeg));
-    if (!tg.empty()) std::memcpy(host.data(), tg.data(), tg.size() * sizeof(TileGate));
-    if (!mats.empty()) std::memcpy(host.data() + b_tg, mats.data(), mats.size() * sizeof(float4));
-    if (!perms.empty()) std::memcpy(host.data() + b_tg + b_m, perms.data(), perms.size() * sizeof(int32_t));
+    if (!segs.empty()) std::memcpy(host + b_tg + b_m + b_p, segs.data(), segs.size() * sizeof(RBSeg));
+    if (!tg.empty()) std::memcpy(host, tg.data(), tg.size() * sizeof(TileGate));
+    if (!mats.empty()) std::memcpy(host + b_tg, mats.data(), mats.size() * sizeof(float4));
+    if (!perms.empty()) std::memcpy(host + b_tg + b_m, perms.data(), perms.size() * sizeof(int32_t));
     if (!big_bits.empty())
-        std::memcpy(host.data() + b_tg + b_m + perms.size() * sizeof(int32_t), big_bits.data(), big_bits.size() * sizeof(int32_t));
+        std::memcpy(host + b_tg + b_m + perms.size() * sizeof(int32_t), big_bits.data(), big_bits.size() * sizeof(int32_t));
     char* dev = (char*)s->plan_buf;
-    rc = bs_cuda_check(s, cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, s->stream), "plan upload");
+    rc = bs_cuda_check(s, cudaMemcpyAsync(dev, host, (size_t)o_tc, cudaMemcpyHostToDevice, s->stream), "plan upload");
+    bs_stage_done(s);
     if (rc) return rc;
     const TileGate* d_tg = (const TileGate*)dev;
     const float4* d_m = (const float4*)(dev + b_tg);
@@ -1289,7 +1292,10 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         d.err = s->dev_flag;
         for (int64_t t0 = 0; t0 < ntiles; t0 += (1LL << 30)) {
             int64_t nb = std::min<int64_t>(ntiles - t0, 1LL << 30);
-            if (ln.tc_last >= 0) {
+            if (ln.tc_last >= 0 && s->capturing) {
+                k_tile_sweep_tc<<<(unsigned)nb, kTcThreads, kTcSmem, s->stream>>>(psi, d, t0, ln.tc_last);
+                s->stats.tc_launches++;
+            } else if (ln.tc_last >= 0) {
                 const size_t pe = 2 * s->tc_events_used;
                 while (s->tc_events.size() < pe + 2) {
                     cudaEvent_t e;

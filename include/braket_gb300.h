@@ -195,6 +195,24 @@ int bs_run_batch(int n_circuits, const int* n_qubits, const bs_op* const* ops, c
                  int n_terms, const uint64_t* xmask, const uint64_t* zmask, int64_t shots, uint64_t seed,
                  int precision, double* expectations_out, int64_t* samples_out, bs_stats* stats_out);
 
+/* ---- captured batches.  The same work as bs_run_batch (same results, same per-circuit shot
+ * seeds), captured once into a CUDA graph and replayed: bs_batch_create runs the batch eagerly once
+ * (sizing a pool of at most four handles, circuits assigned largest-first), then captures every
+ * upload, kernel and result copy of the batch into one graph; bs_batch_launch replays it and
+ * copies the results out (host work per replay: one graph launch and two memcpy).
+ * bs_batch_set_ops replaces every circuit's ops (same qubit counts; a circuit may not move
+ * between the small-circuit kernel and the tile path), recaptures, and updates the executable
+ * graph in place when its topology is unchanged (re-instantiates it otherwise) — the path for
+ * parameter sweeps.  A replay repeats the same shot seeds.  No reference counterpart: the
+ * reference's batch (src/BraketSimulator.jl:347-395) spawns Julia tasks per call. */
+typedef struct bs_batch bs_batch;
+int bs_batch_create(int n_circuits, const int* n_qubits, const bs_op* const* ops, const int64_t* n_ops,
+                    int n_terms, const uint64_t* xmask, const uint64_t* zmask, int64_t shots, uint64_t seed,
+                    int precision, bs_batch** out);
+int bs_batch_set_ops(bs_batch* batch, const bs_op* const* ops, const int64_t* n_ops);
+int bs_batch_launch(bs_batch* batch, double* expectations_out, int64_t* samples_out, bs_stats* stats_out);
+int bs_batch_destroy(bs_batch* batch);
+
 /* synchronise the handle's stream; device pointer of the state (for in-HBM benchmarking) */
 int bs_synchronize(bs_sim* sim);
 int bs_state_device_ptr(bs_sim* sim, void** out);

@@ -72,3 +72,61 @@ def test_batch_small_circuits_share_one_launch():
     for c in range(64):
         e, _ = exact(circuits[c], counts[c], obs[c])
         assert np.max(np.abs(exp[c] - e)) < 2e-5
+
+
+def rebind_angles(circuits, rng):
+    """Same gate sequence, new rotation angles (a parameter sweep)."""
+    out = []
+    for ins in circuits:
+        new = []
+        for ix in ins:
+            op = ix.operator
+            if isinstance(op, (bs.Rx, bs.Ry, bs.Rz)):
+                op = type(op)(float(rng.uniform(-np.pi, np.pi)))
+            new.append(bs.Instruction(op, list(ix.target)))
+        out.append(new)
+    return out
+
+
+@pytest.mark.parametrize("precision", ["c64", "c128"])
+def test_captured_batch_replays_the_one_shot_results(precision):
+    rng = np.random.default_rng(21)
+    circuits, counts, obs = random_batch(24, 3, 16, rng)
+    shots = 500
+    exp1, smp1, _ = bs.batch_simulate(circuits, counts, obs, shots=shots, seed=9, precision=precision)
+    with bs.CapturedBatch(circuits, counts, obs, shots=shots, seed=9, precision=precision) as cb:
+        for _ in range(3):
+            exp2, smp2, st = cb.launch()
+            # the same kernels on the same inputs: identical expectations and shots
+            assert np.array_equal(exp1, exp2)
+            assert np.array_equal(smp1, smp2)
+            assert st["gpu_ms"] > 0
+
+
+def test_captured_batch_parameter_update():
+    rng = np.random.default_rng(5)
+    circuits, counts, obs = random_batch(20, 2, 15, rng)
+    with bs.CapturedBatch(circuits, counts, obs, shots=64, seed=2, precision="c128") as cb:
+        for _ in range(2):
+            circuits = rebind_angles(circuits, rng)
+            cb.set_circuits(circuits)
+            exp, smp, _ = cb.launch()
+            ref, _, _ = bs.batch_simulate(circuits, counts, obs, shots=64, seed=2, precision="c128")
+            assert np.array_equal(exp, ref)
+            for c in range(len(circuits)):
+                e, _ = exact(circuits[c], counts[c], obs[c])
+                assert np.max(np.abs(exp[c] - e)) < 1e-12
+
+
+def test_captured_batch_rejects_a_change_of_path():
+    rng = np.random.default_rng(8)
+    circuits, counts, obs = random_batch(6, 3, 8, rng)
+    with bs.CapturedBatch(circuits, counts, obs, shots=0, seed=0, precision="c64") as cb:
+        changed = [list(ins) for ins in circuits]
+        # a 2-qubit dense gate moves a small circuit from the one-CTA kernel to the tile path
+        changed[0].append(bs.Instruction(bs.XX(0.3), [0, 1]))
+        with pytest.raises(bs._abi.BraketGB300Error):
+            cb.set_circuits(changed)
+        exp, _, _ = cb.launch()   # the batch is still usable
+        ref, _, _ = bs.batch_simulate(circuits, counts, obs, shots=0, seed=0, precision="c64")
+        assert np.array_equal(exp, ref)
