@@ -19,6 +19,7 @@ from .results import (Amplitude, DensityMatrix, Expectation, Probability, Sample
 from .adjoint import adjoint_gradient, parameter_shift_gradient  # noqa: F401
 from .program import Program, simulate, create_sim  # noqa: F401
 from .batch import CapturedBatch, batch_simulate  # noqa: F401
+from .autotune import autotune, get_tuning, set_tuning  # noqa: F401
 
 
 def library_path() -> str:

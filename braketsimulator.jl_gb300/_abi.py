@@ -19,6 +19,7 @@ BS_GATE_SORTED_TARGETS = 0x04
 BS_GATE_MSB_FIRST = 0x08
 BS_NOISE_REFERENCE = 0x00
 BS_NOISE_PHYSICAL = 0x10
+BS_TUNE_TILE_BITS, BS_TUNE_TILE_THREADS, BS_TUNE_TC, BS_TUNE_TC_MIN_BITS, BS_TUNE_TC_COST = 0, 1, 2, 3, 4
 BS_MAX_TARGETS = 10
 BS_MAX_CONTROLS = 16
 
@@ -97,6 +98,8 @@ SIGNATURES = {
     "bs_batch_set_ops": (_i32, [_p, _P(_P(BsOp)), _P(_i64)]),
     "bs_batch_launch": (_i32, [_p, _P(_f64), _P(_i64), _P(BsStats)]),
     "bs_batch_destroy": (_i32, [_p]),
+    "bs_set_tuning": (_i32, [_p, _i32, _f64]),
+    "bs_get_tuning": (_i32, [_p, _i32, _P(_f64)]),
     "bs_synchronize": (_i32, [_p]),
     "bs_state_device_ptr": (_i32, [_p, _P(_p)]),
 }

@@ -193,6 +193,49 @@ int bs_destroy(bs_sim* s) {
     return BS_OK;
 }
 
+int bs_set_tuning(bs_sim* s, int param, double value) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    const bool reset = value < 0;
+    const int iv = (int)value;
+    switch (param) {
+        case BS_TUNE_TILE_BITS:
+            if (!reset && (iv < 10 || iv > BS_TILE_MAX_BITS || iv != value)) break;
+            s->tune.tile_bits = reset ? -1 : iv;
+            return BS_OK;
+        case BS_TUNE_TILE_THREADS:
+            if (!reset && iv != 256 && iv != 512) break;
+            s->tune.tile_threads = reset ? -1 : iv;
+            return BS_OK;
+        case BS_TUNE_TC:
+            if (!reset && iv != 0 && iv != 1) break;
+            s->tune.tc = reset ? -1 : iv;
+            return BS_OK;
+        case BS_TUNE_TC_MIN_BITS:
+            if (!reset && (iv > 64 || iv != value)) break;
+            s->tune.tc_min_bits = reset ? -1 : iv;
+            return BS_OK;
+        case BS_TUNE_TC_COST:
+            if (!reset && !(value < 1e9)) break;
+            s->tune.tc_cost = reset ? -1.0 : value;
+            return BS_OK;
+        default:
+            return bs_fail(s, BS_ERR_INVALID_ARG, "unknown tuning parameter");
+    }
+    return bs_fail(s, BS_ERR_INVALID_ARG, "tuning value out of range");
+}
+
+int bs_get_tuning(bs_sim* s, int param, double* value) {
+    if (!s || !value) return BS_ERR_INVALID_ARG;
+    switch (param) {
+        case BS_TUNE_TILE_BITS: *value = bs_tile_bits(s); return BS_OK;
+        case BS_TUNE_TILE_THREADS: *value = bs_tile_threads(s); return BS_OK;
+        case BS_TUNE_TC: *value = bs_tc_enabled(s) ? 1.0 : 0.0; return BS_OK;
+        case BS_TUNE_TC_MIN_BITS: *value = bs_tc_min_bits(s); return BS_OK;
+        case BS_TUNE_TC_COST: *value = bs_tc_cost(s); return BS_OK;
+        default: return bs_fail(s, BS_ERR_INVALID_ARG, "unknown tuning parameter");
+    }
+}
+
 int bs_reinit(bs_sim* s, int n_qubits) {
     if (!ok_handle(s)) return BS_ERR_INVALID_ARG;
     return alloc_state(s, n_qubits);
@@ -274,7 +317,7 @@ int bs_apply_gate(bs_sim* s, const double* matrix, int k, const int* targets, in
     int rc = bs_lower_gate(s, matrix, k, targets, nc, controls, cvals, flags, s->kind == BS_KIND_DM, hg);
     if (rc) return rc;
     std::vector<Sweep> sw;
-    bs_plan_sweeps(hg, bs_vec_bits(s), sw);
+    bs_plan_sweeps(hg, bs_vec_bits(s), bs_tile_bits(s), sw);
     s->alias_valid = false;
     return bs_run_sweeps(s, sw);
 }
@@ -287,7 +330,7 @@ int bs_dm_apply_vec_gate(bs_sim* s, const double* matrix, int k, const int* targ
     int rc = bs_lower_gate(s, matrix, k, targets, nc, controls, cvals, flags, false, hg);
     if (rc) return rc;
     std::vector<Sweep> sw;
-    bs_plan_sweeps(hg, bs_vec_bits(s), sw);
+    bs_plan_sweeps(hg, bs_vec_bits(s), bs_tile_bits(s), sw);
     s->alias_valid = false;
     return bs_run_sweeps(s, sw);
 }
@@ -302,7 +345,7 @@ int bs_apply_kraus(bs_sim* s, const double* kraus, int nk, int k, const int* tar
         int rc = bs_lower_kraus_physical(s, kraus, nk, k, targets, flags, hg);
         if (rc) return rc;
         std::vector<Sweep> sw;
-        bs_plan_sweeps(hg, bs_vec_bits(s), sw);
+        bs_plan_sweeps(hg, bs_vec_bits(s), bs_tile_bits(s), sw);
         return bs_run_sweeps(s, sw);
     }
     return bs_kraus_reference(s, kraus, nk, k, targets, flags);
@@ -319,7 +362,7 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     auto flush = [&]() -> int {
         if (pending.empty()) return BS_OK;
         std::vector<Sweep> sw;
-        bs_plan_sweeps(pending, bs_vec_bits(s), sw);
+        bs_plan_sweeps(pending, bs_vec_bits(s), bs_tile_bits(s), sw);
         pending.clear();
         return bs_run_sweeps(s, sw);
     };

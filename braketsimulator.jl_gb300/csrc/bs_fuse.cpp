@@ -113,22 +113,10 @@ struct Block {
     double cost = 0;
 };
 
-double tc_cost() {
-    const char* v = getenv("BS_TC_COST");
-    return v ? atof(v) : 2.0;
-}
-
 }  // namespace
 
-// BS_TC=0 keeps every gate on the float-float path (read on every call, so a process can compare both)
-bool bs_tc_enabled() {
-    const char* v = getenv("BS_TC");
-    return !(v && v[0] == '0');
-}
-
-void bs_fuse_tc(const std::vector<HostGate>& in, const int* local, int T, std::vector<HostGate>& out) {
+void bs_fuse_tc(const std::vector<HostGate>& in, const int* local, int T, double threshold, std::vector<HostGate>& out) {
     out.clear();
-    const double threshold = tc_cost();
     std::vector<Block> open;
     auto emit = [&](Block& b) {
         int ndense = 0;

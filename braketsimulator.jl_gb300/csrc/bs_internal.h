@@ -71,6 +71,16 @@ struct Sweep {
     std::vector<HostGate> gates;
 };
 
+// Per-handle tuning (bs_set_tuning); a negative value means "environment variable, else the
+// built-in default" (BS_TILE_BITS 12, BS_TILE_THREADS 256, BS_TC 1, BS_TC_MIN_BITS 22, BS_TC_COST 2).
+struct BsTuning {
+    int tile_bits = -1;      // tile bits of the sweep kernels, 10..12
+    int tile_threads = -1;   // threads per CTA of the float-float sweep kernel, 256 or 512
+    int tc = -1;             // fused tensor-core sweeps on (1) or off (0)
+    int tc_min_bits = -1;    // vector bits from which fused tensor-core sweeps are used
+    double tc_cost = -1;     // float-float cost (dense 1-qubit gates) above which a block is fused
+};
+
 struct bs_sim {
     int kind = BS_KIND_SV;
     int n = 0;                    // qubits
@@ -96,6 +106,7 @@ struct bs_sim {
     std::vector<cudaEvent_t> tc_events;   // pool: an event pair around each tensor-core launch
     size_t tc_events_used = 0;            // pairs recorded since the last bs_collect_tc_time
     bs_stats stats{};
+    BsTuning tune{};
     std::string err;
     // Host staging of uploads: pinned, reused once the previous upload has landed (hstage_ev).
     char* hstage = nullptr;
@@ -130,16 +141,18 @@ int bs_lower_gate(bs_sim* s, const double* matrix, int k, const int* targets, in
                   std::vector<HostGate>& out);
 int bs_lower_kraus_physical(bs_sim* s, const double* kraus, int nk, int k, const int* targets,
                             unsigned flags, std::vector<HostGate>& out);
-void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, std::vector<Sweep>& out);
-// Tile geometry: tile bits (10..12, env BS_TILE_BITS) and threads per CTA (256/512, env BS_TILE_THREADS)
-int bs_tile_bits();
-int bs_tile_threads();
+void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, int tile_bits, std::vector<Sweep>& out);
+// Tuned values of a handle (its setting, else the environment, else the default)
+int bs_tile_bits(const bs_sim* s);
+int bs_tile_threads(const bs_sim* s);
+bool bs_tc_enabled(const bs_sim* s);
+int bs_tc_min_bits(const bs_sim* s);
+double bs_tc_cost(const bs_sim* s);
 
 // ---- tensor-core fusion (bs_fuse.cpp)
-bool bs_tc_enabled();
-// Fold runs of in-tile gates into kind-4 HostGates (5 endian bits, 32x32 matrix) where that is cheaper.
-// local[e]: tile position of endian bit e or -1.
-void bs_fuse_tc(const std::vector<HostGate>& in, const int* local, int T, std::vector<HostGate>& out);
+// Fold runs of in-tile gates into kind-4 HostGates (5 endian bits, 32x32 matrix) where that is cheaper
+// (float-float cost above `threshold`).  local[e]: tile position of endian bit e or -1.
+void bs_fuse_tc(const std::vector<HostGate>& in, const int* local, int T, double threshold, std::vector<HostGate>& out);
 // Smallest eu with every entry of the n_mat 32x32 matrices below 2^eu; false if not finite or above 2^12.
 bool bs_tc_exponent(const double* mat, int n_mat, int& eu);
 

@@ -174,29 +174,47 @@ int bs_lower_kraus_physical(bs_sim* s, const double* kraus, int nk, int k, const
     return BS_OK;
 }
 
-int bs_tile_bits() {
-    static const int v = [] {
+int bs_tile_bits(const bs_sim* s) {
+    int b = s ? s->tune.tile_bits : -1;
+    if (b < 0) {
         const char* e = getenv("BS_TILE_BITS");
-        int b = e ? atoi(e) : BS_TILE_MAX_BITS;
-        return (b >= 10 && b <= BS_TILE_MAX_BITS) ? b : BS_TILE_MAX_BITS;
-    }();
-    return v;
+        b = e ? atoi(e) : BS_TILE_MAX_BITS;
+    }
+    return (b >= 10 && b <= BS_TILE_MAX_BITS) ? b : BS_TILE_MAX_BITS;
 }
 
-int bs_tile_threads() {
-    static const int v = [] {
+int bs_tile_threads(const bs_sim* s) {
+    int t = s ? s->tune.tile_threads : -1;
+    if (t < 0) {
         const char* e = getenv("BS_TILE_THREADS");
-        int t = e ? atoi(e) : 256;
-        return (t == 512) ? 512 : 256;
-    }();
-    return v;
+        t = e ? atoi(e) : 256;
+    }
+    return (t == 512) ? 512 : 256;
+}
+
+bool bs_tc_enabled(const bs_sim* s) {
+    if (s && s->tune.tc >= 0) return s->tune.tc != 0;
+    const char* v = getenv("BS_TC");   // read on every call, so a process can compare both paths
+    return !(v && v[0] == '0');
+}
+
+int bs_tc_min_bits(const bs_sim* s) {
+    if (s && s->tune.tc_min_bits >= 0) return s->tune.tc_min_bits;
+    const char* v = getenv("BS_TC_MIN_BITS");
+    return v ? atoi(v) : 22;   // measured wins from 24 bits up; small states are bound by host planning
+}
+
+double bs_tc_cost(const bs_sim* s) {
+    if (s && s->tune.tc_cost >= 0) return s->tune.tc_cost;
+    const char* v = getenv("BS_TC_COST");
+    return v ? atof(v) : 2.0;
 }
 
 // Greedy sweep planner.  A gate may move ahead of gates it does not share a bit
 // with; a dense or monomial gate needs its target bits inside the tile, a
 // diagonal gate or a control never does (their bits are read from the index).
-void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, std::vector<Sweep>& out) {
-    const int T = std::min(bs_tile_bits(), n_bits);
+void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, int tile_bits, std::vector<Sweep>& out) {
+    const int T = std::min(tile_bits, n_bits);
     const int L = std::min(BS_TILE_LOW_BITS, T);
     const int cap = T - L;
     const size_t G = gates.size();

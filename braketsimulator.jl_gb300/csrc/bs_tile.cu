@@ -961,7 +961,7 @@ inline float4 to_cff(double re, double im) {
 int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     if (sweeps.empty()) return BS_OK;
     const int n_bits = bs_vec_bits(s);
-    const int T = std::min(bs_tile_bits(), n_bits);
+    const int T = std::min(bs_tile_bits(s), n_bits);
     const int L = std::min(BS_TILE_LOW_BITS, T);
     // pack: per sweep [TileGate...], then one float4 pool, then one int pool
     std::vector<TileGate> tg;
@@ -977,11 +977,10 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     std::vector<double> tc_mats, tc_scale;   // fused matrices (complex 32x32 per variant), 2^(7-eu) per variant
     int64_t n_var = 0;
     const bool c64 = s->precision == BS_PREC_C64;
-    // fused tensor-core sweeps from 22 vector bits up (measured wins at 24, 26, 28 and 30 bits;
-    // small states are dominated by host planning); BS_TC_MIN_BITS overrides the threshold
-    const char* tmb = getenv("BS_TC_MIN_BITS");
-    const int tc_min_bits = tmb ? atoi(tmb) : 22;
-    const bool use_tc = bs_tc_enabled() && !c64 && T == 12 && L == 5 && n_bits >= tc_min_bits;
+    // fused tensor-core sweeps from bs_tc_min_bits vector bits up (22 by default: measured wins at
+    // 24, 26, 28 and 30 bits; small states are dominated by host planning)
+    const bool use_tc = bs_tc_enabled(s) && !c64 && T == 12 && L == 5 && n_bits >= bs_tc_min_bits(s);
+    const double tc_threshold = bs_tc_cost(s);
     // fusion per sweep (independent, so on a few host threads); a sweep left with unfused 3/4-target
     // gates or with reference-mode channels keeps its plain gate list, since the tensor-core sweep
     // kernel carries float-float paths for 1- and 2-target gates only
@@ -996,7 +995,7 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
                 for (int b = 0; b < 64; b++) local[b] = -1;
                 for (int b = 0; b < L; b++) local[b] = b;
                 for (size_t q = 0; q < sw.hi_bits.size(); q++) local[sw.hi_bits[q]] = L + (int)q;
-                bs_fuse_tc(sw.gates, local, T, fused_all[i]);
+                bs_fuse_tc(sw.gates, local, T, tc_threshold, fused_all[i]);
                 bool ok = true;
                 for (const HostGate& hg : fused_all[i])
                     if ((hg.kind != 1 && hg.kind != 4 && hg.k >= 3) || hg.kind == 5) ok = false;
@@ -1316,7 +1315,7 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
                 k_tile_rb<1><<<(unsigned)nb, kThreads, smem, s->stream>>>(psi, d, d_seg + seg0[li], (int)nseg[li], t0);
             else if (seg0[li] >= 0)
                 k_tile_rb<2><<<(unsigned)nb, kThreads, smem, s->stream>>>(psi, d, d_seg + seg0[li], (int)nseg[li], t0);
-            else if (bs_tile_threads() == 512) {
+            else if (bs_tile_threads(s) == 512) {
                 if (ln.kmax <= 2) k_tile_sweep<2, 512><<<(unsigned)nb, 512, smem, s->stream>>>(psi, d, t0);
                 else k_tile_sweep<4, 512><<<(unsigned)nb, 512, smem, s->stream>>>(psi, d, t0);
             } else {

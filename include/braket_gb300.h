@@ -213,6 +213,23 @@ int bs_batch_set_ops(bs_batch* batch, const bs_op* const* ops, const int64_t* n_
 int bs_batch_launch(bs_batch* batch, double* expectations_out, int64_t* samples_out, bs_stats* stats_out);
 int bs_batch_destroy(bs_batch* batch);
 
+/* ---- per-handle tuning, set by the project's autotuner (braketsimulator_gb300.autotune) or by hand.
+ * No reference counterpart (the reference has no tunable kernels).  A negative value restores
+ * "environment variable, else built-in default"; bs_get_tuning returns the value in effect.
+ *   BS_TUNE_TILE_BITS     10..12  amplitude bits per tile of the sweep kernels (BS_TILE_BITS)
+ *   BS_TUNE_TILE_THREADS  256|512 threads per CTA of the float-float sweep (BS_TILE_THREADS)
+ *   BS_TUNE_TC            0|1     fused tensor-core sweeps (BS_TC)
+ *   BS_TUNE_TC_MIN_BITS   n       vector bits from which they are used (BS_TC_MIN_BITS, 22)
+ *   BS_TUNE_TC_COST       x       fuse a block when its float-float cost (dense 1-qubit gates)
+ *                                 exceeds x (BS_TC_COST, 2) */
+#define BS_TUNE_TILE_BITS     0
+#define BS_TUNE_TILE_THREADS  1
+#define BS_TUNE_TC            2
+#define BS_TUNE_TC_MIN_BITS   3
+#define BS_TUNE_TC_COST       4
+int bs_set_tuning(bs_sim* sim, int param, double value);
+int bs_get_tuning(bs_sim* sim, int param, double* value);
+
 /* synchronise the handle's stream; device pointer of the state (for in-HBM benchmarking) */
 int bs_synchronize(bs_sim* sim);
 int bs_state_device_ptr(bs_sim* sim, void** out);
