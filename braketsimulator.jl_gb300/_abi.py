@@ -98,6 +98,7 @@ SIGNATURES = {
     "bs_batch_set_ops": (_i32, [_p, _P(_P(BsOp)), _P(_i64)]),
     "bs_batch_launch": (_i32, [_p, _P(_f64), _P(_i64), _P(BsStats)]),
     "bs_batch_destroy": (_i32, [_p]),
+    "bs_batch_set_tuning": (_i32, [_p, _i32, _P(_i32), _P(_f64)]),
     "bs_set_tuning": (_i32, [_p, _i32, _f64]),
     "bs_get_tuning": (_i32, [_p, _i32, _P(_f64)]),
     "bs_synchronize": (_i32, [_p]),

@@ -101,6 +101,41 @@ class CapturedBatch:
         if rc != 0:
             raise _abi.BraketGB300Error(rc, "bs_batch_set_ops failed")
 
+    def set_tuning(self, **values):
+        """Tunables (see ``autotune.PARAMS``) on every handle of the batch, then a graph rebuild;
+        None restores the environment / default value."""
+        from .autotune import PARAMS
+        for name in values:
+            if name not in PARAMS:
+                raise KeyError(f"unknown tunable {name!r}")
+        ids = np.array([PARAMS[k] for k in values], dtype=np.int32)
+        vals = np.array([-1.0 if v is None else float(v) for v in values.values()], dtype=np.float64)
+        rc = _abi.lib().bs_batch_set_tuning(self._h, len(ids), _abi.iptr(ids), _abi.dptr(vals))
+        if rc != 0:
+            raise _abi.BraketGB300Error(rc, "bs_batch_set_tuning failed")
+
+    def autotune(self, candidates=None, repeats: int = 2) -> dict:
+        """Time replays under each candidate setting (default: tile bits x sweep threads, and for
+        complex128 the tensor-core fusion widths) and keep the fastest."""
+        import time
+        from .autotune import PARAMS
+        if candidates is None:
+            candidates = [{"tile_bits": tb, "tile_threads": thr, "tc": 0} for tb in (10, 11, 12) for thr in (256, 512)]
+            candidates += [{"tile_bits": 12, "tc": 1, "tc_min_bits": 0, "tc_cost": c} for c in (1.0, 2.0, 4.0)]
+        timings = []
+        for cand in candidates:
+            self.set_tuning(**{**{k: None for k in PARAMS}, **cand})
+            self.launch()
+            best = float("inf")
+            for _ in range(max(1, repeats)):
+                t0 = time.perf_counter()
+                self.launch()
+                best = min(best, time.perf_counter() - t0)
+            timings.append({"setting": cand, "seconds": best})
+        win = min(timings, key=lambda r: r["seconds"])
+        self.set_tuning(**{**{k: None for k in PARAMS}, **win["setting"]})
+        return {"setting": win["setting"], "seconds": win["seconds"], "timings": timings}
+
     def launch(self):
         """Replay; returns (expectations [n_circuits, n_terms], samples [n_circuits, shots], stats)."""
         exp = np.zeros(max(1, self.nc * self.n_terms), dtype=np.float64)

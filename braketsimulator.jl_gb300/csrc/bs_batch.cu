@@ -462,6 +462,11 @@ struct bs_batch {
     cudaGraphExec_t exec = nullptr;
     bs_stats st{};
     std::vector<std::vector<std::pair<char*, size_t>>> arena_old;
+    // a copy of the current ops (and their matrices), for rebuilds after a tuning change
+    std::vector<std::vector<bs_op>> ops;
+    std::vector<std::vector<double>> mats;
+    std::vector<const bs_op*> op_ptrs;
+    std::vector<int64_t> n_ops;
 };
 
 namespace {
@@ -469,6 +474,33 @@ namespace {
 void free_pinned(char*& p) {
     if (p) cudaFreeHost(p);
     p = nullptr;
+}
+
+// Keep a deep copy of the circuits' ops (matrix data included).
+void batch_store_ops(bs_batch* b, const bs_op* const* ops, const int64_t* n_ops) {
+    b->ops.assign((size_t)b->nc, {});
+    b->mats.assign((size_t)b->nc, {});
+    b->op_ptrs.assign((size_t)b->nc, nullptr);
+    b->n_ops.assign(n_ops, n_ops + b->nc);
+    for (int c = 0; c < b->nc; c++) {
+        std::vector<size_t> off;
+        for (int64_t i = 0; i < n_ops[c]; i++) {
+            const bs_op& o = ops[c][i];
+            off.push_back(b->mats[(size_t)c].size());
+            if (o.kind == 2 || !o.matrix) continue;
+            const int d = 1 << o.n_targets;
+            size_t len;
+            if (o.kind == 1) len = (size_t)std::max(o.n_matrices, 1) * d * d * 2;
+            else len = (o.flags & BS_GATE_DIAGONAL) ? (size_t)d * 2 : (size_t)d * d * 2;
+            b->mats[(size_t)c].insert(b->mats[(size_t)c].end(), o.matrix, o.matrix + len);
+        }
+        b->ops[(size_t)c].assign(ops[c], ops[c] + n_ops[c]);
+        for (int64_t i = 0; i < n_ops[c]; i++) {
+            bs_op& o = b->ops[(size_t)c][(size_t)i];
+            if (o.kind != 2 && o.matrix) o.matrix = b->mats[(size_t)c].data() + off[(size_t)i];
+        }
+        b->op_ptrs[(size_t)c] = b->ops[(size_t)c].data();
+    }
 }
 
 // Pack the small circuits of ops into a fresh pinned image (the previous one stays alive in
@@ -694,7 +726,10 @@ int bs_batch_create(int n_circuits, const int* n_qubits, const bs_op* const* ops
     }
     if (!rc && n_terms && cudaMallocHost(&b->exp_pin, (size_t)n_circuits * n_terms * 8) != cudaSuccess) rc = BS_ERR_ALLOC;
     if (!rc && shots && cudaMallocHost(&b->samp_pin, (size_t)n_circuits * shots * 8) != cudaSuccess) rc = BS_ERR_ALLOC;
-    if (!rc) rc = batch_build(b, ops, n_ops, true);
+    if (!rc) {
+        batch_store_ops(b, ops, n_ops);
+        rc = batch_build(b, b->op_ptrs.data(), b->n_ops.data(), true);
+    }
     if (rc) {
         bs_batch_destroy(b);
         return rc;
@@ -711,7 +746,18 @@ int bs_batch_set_ops(bs_batch* b, const bs_op* const* ops, const int64_t* n_ops)
         const bool sm = small_ok(b->precision, b->nq[(size_t)c], ops[c], n_ops[c]);
         if (sm != (b->owner[(size_t)c] < 0)) return BS_ERR_INVALID_ARG;
     }
-    return batch_build(b, ops, n_ops, false);
+    batch_store_ops(b, ops, n_ops);
+    return batch_build(b, b->op_ptrs.data(), b->n_ops.data(), false);
+}
+
+int bs_batch_set_tuning(bs_batch* b, int n, const int* params, const double* values) {
+    if (!b || n < 0 || (n > 0 && (!params || !values))) return BS_ERR_INVALID_ARG;
+    for (bs_sim* s : b->h)
+        for (int i = 0; i < n; i++) {
+            const int rc = bs_set_tuning(s, params[i], values[i]);
+            if (rc) return rc;
+        }
+    return batch_build(b, b->op_ptrs.data(), b->n_ops.data(), false);
 }
 
 int bs_batch_launch(bs_batch* b, double* expectations_out, int64_t* samples_out, bs_stats* stats_out) {

@@ -229,6 +229,9 @@ int bs_batch_destroy(bs_batch* batch);
 #define BS_TUNE_TC_COST       4
 int bs_set_tuning(bs_sim* sim, int param, double value);
 int bs_get_tuning(bs_sim* sim, int param, double* value);
+/* n settings (params[i] = values[i]) on every handle of a captured batch, then one rebuild of its
+ * graph (the batch keeps a copy of its circuits for this) */
+int bs_batch_set_tuning(bs_batch* batch, int n, const int* params, const double* values);
 
 /* synchronise the handle's stream; device pointer of the state (for in-HBM benchmarking) */
 int bs_synchronize(bs_sim* sim);

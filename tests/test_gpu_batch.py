@@ -130,3 +130,16 @@ def test_captured_batch_rejects_a_change_of_path():
         exp, _, _ = cb.launch()   # the batch is still usable
         ref, _, _ = bs.batch_simulate(circuits, counts, obs, shots=0, seed=0, precision="c64")
         assert np.array_equal(exp, ref)
+
+
+def test_captured_batch_autotune_keeps_results():
+    rng = np.random.default_rng(31)
+    circuits, counts, obs = random_batch(12, 10, 16, rng)
+    ref, smp_ref, _ = bs.batch_simulate(circuits, counts, obs, shots=200, seed=4, precision="c128")
+    with bs.CapturedBatch(circuits, counts, obs, shots=200, seed=4, precision="c128") as cb:
+        res = cb.autotune(repeats=1)
+        assert res["setting"] in [t["setting"] for t in res["timings"]]
+        exp, smp, _ = cb.launch()
+        # every tuning computes the same state to 1e-12; shots may differ only at exact CDF ties
+        assert np.max(np.abs(exp - ref)) < 1e-11
+        assert np.mean(smp == smp_ref) > 0.99
