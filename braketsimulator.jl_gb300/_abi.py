@@ -20,6 +20,7 @@ BS_GATE_MSB_FIRST = 0x08
 BS_NOISE_REFERENCE = 0x00
 BS_NOISE_PHYSICAL = 0x10
 BS_TUNE_TILE_BITS, BS_TUNE_TILE_THREADS, BS_TUNE_TC, BS_TUNE_TC_MIN_BITS, BS_TUNE_TC_COST = 0, 1, 2, 3, 4
+BS_TUNE_ADJ_SEGMENTS = 5
 BS_MAX_TARGETS = 10
 BS_MAX_CONTROLS = 16
 

@@ -140,3 +140,38 @@ def finite_difference_gradient(sim, instructions, hamiltonian, h: float = 1e-6):
         e0 = energy(sim, instructions[:i] + [dn] + instructions[i + 1:], hamiltonian)
         grad[slot] = (e1 - e0) / (2 * h)
     return grad
+
+
+def energy_rrule(sim: StateVectorSimulator, instructions: Sequence[Instruction], hamiltonian,
+                 param_index: Sequence[int] | None = None):
+    """Reverse-mode rule for <H>(theta) in the form of a ChainRulesCore ``rrule``: returns
+    ``(energy, pullback)`` where ``pullback(de)`` gives the cotangent of every parameter slot,
+    ``de * d<H>/dtheta``.  One adjoint evaluation serves both."""
+    e, g = adjoint_gradient(sim, instructions, hamiltonian, param_index)
+
+    def pullback(de):
+        return float(de) * g
+
+    return e, pullback
+
+
+def torch_energy(build, hamiltonian, sim: StateVectorSimulator):
+    """A torch.autograd function theta -> <H>(theta): ``build(theta: np.ndarray)`` returns the
+    instruction list whose differentiable gates take theta in order of appearance.  Forward runs
+    the adjoint method once; backward returns grad_output * gradient (device-independent: theta may
+    live anywhere, the engine is called with host values)."""
+    import torch
+
+    class _Energy(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, theta):
+            e, g = adjoint_gradient(sim, build(theta.detach().double().cpu().numpy()), hamiltonian)
+            ctx.save_for_backward(torch.as_tensor(g, dtype=theta.dtype, device=theta.device))
+            return theta.new_tensor(e)
+
+        @staticmethod
+        def backward(ctx, grad_output):
+            (g,) = ctx.saved_tensors
+            return grad_output * g
+
+    return _Energy.apply

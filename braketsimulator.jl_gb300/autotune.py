@@ -9,7 +9,9 @@ no tunable kernels):
 * ``tc`` (0 / 1): fused tensor-core sweeps;
 * ``tc_min_bits``: vector bits from which fused tensor-core sweeps are used;
 * ``tc_cost``: fusion width — a run of gates on at most 5 tile bits becomes one fused unitary when
-  its float-float cost (in dense 1-qubit gates) exceeds this.
+  its float-float cost (in dense 1-qubit gates) exceeds this;
+* ``adj_segments``: adjoint gradients' forward segments (checkpoints of psi + 1); not timed by
+  ``autotune`` (it trades memory for accuracy, not speed).
 
 ``autotune(sim, instructions)`` re-initialises the simulator, times ``evolve`` of the instructions
 (wall clock: host planning included) under each candidate, leaves the fastest set on the handle
@@ -27,7 +29,8 @@ import time
 from . import _abi
 
 PARAMS = {"tile_bits": _abi.BS_TUNE_TILE_BITS, "tile_threads": _abi.BS_TUNE_TILE_THREADS,
-          "tc": _abi.BS_TUNE_TC, "tc_min_bits": _abi.BS_TUNE_TC_MIN_BITS, "tc_cost": _abi.BS_TUNE_TC_COST}
+          "tc": _abi.BS_TUNE_TC, "tc_min_bits": _abi.BS_TUNE_TC_MIN_BITS, "tc_cost": _abi.BS_TUNE_TC_COST,
+          "adj_segments": _abi.BS_TUNE_ADJ_SEGMENTS}
 
 _CACHE: dict = {}
 

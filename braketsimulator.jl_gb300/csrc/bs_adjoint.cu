@@ -11,6 +11,14 @@
 // Both backward states are swept together: one tile sweep loads the same tile of
 // psi and lambda, applies the daggered gates of a run to both, and accumulates
 // the inner products of the run's parameterised gates before applying them.
+//
+// Checkpoints: the forward pass runs in S segments and keeps psi after each of the
+// first S-1; the backward pass, entering a segment, replaces the uncomputed psi by
+// that checkpoint, so the rounding drift of uncomputation never spans more than
+// one segment.  S comes from the handle's tuning (BS_TUNE_ADJ_SEGMENTS) or, by
+// default, from the parameterised gate count and a quarter of the free device
+// memory; when memory binds (an allocation fails) S is halved down to 1, pure
+// uncomputation.
 #include <algorithm>
 #include <complex>
 #include <cstring>
@@ -330,14 +338,73 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
         for (int q = 0; q < n; q++) if ((m >> q) & 1ULL) e |= 1ULL << (n - 1 - q);
         return e;
     };
-    // 1. forward pass
-    int rc = bs_evolve(s, ops, n_ops, 0);
-    if (rc) return rc;
+    // 0. segments and checkpoint buffers
+    int n_param_gates = 0;
+    for (int64_t i = 0; i < n_ops; i++) n_param_gates += (ops[i].kind == 0 && param_index[i] >= 0) ? 1 : 0;
+    int S = s->tune.adj_segments;
+    const size_t state_bytes = (size_t)len * esz;
+    if (S < 0) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        const int by_mem = (int)std::min<size_t>(64, fr / 4 / std::max<size_t>(state_bytes, 1));
+        S = std::min(std::min(16, 1 + n_param_gates / 16), by_mem + 1);
+    }
+    S = std::max(1, std::min<int>(S, (int)std::max<int64_t>(1, n_ops)));
+    std::vector<void*> ckpt;
+    for (;;) {
+        bool ok = true;
+        for (int j = 0; j + 1 < S; j++) {
+            void* p = nullptr;
+            if (cudaMalloc(&p, state_bytes) != cudaSuccess) { ok = false; break; }
+            ckpt.push_back(p);
+        }
+        if (ok) break;
+        cudaGetLastError();
+        for (void* p : ckpt) cudaFree(p);
+        ckpt.clear();
+        S = std::max(1, S / 2);   // memory binds: fewer checkpoints, more uncomputation
+        if (S == 1) break;
+    }
+    auto free_ckpt = [&]() { for (void* p : ckpt) cudaFree(p); ckpt.clear(); };
+    // segment j covers ops [seg[j], seg[j+1]), split evenly by gate count
+    std::vector<int64_t> seg(1, 0);
+    {
+        int64_t n_gates = 0;
+        for (int64_t i = 0; i < n_ops; i++) n_gates += ops[i].kind == 0;
+        int64_t cnt = 0;
+        for (int64_t i = 0; i < n_ops && (int)seg.size() < S; i++) {
+            cnt += ops[i].kind == 0;
+            if (cnt * S >= n_gates * (int64_t)seg.size() && i + 1 < n_ops) seg.push_back(i + 1);
+        }
+        seg.push_back(n_ops);
+        S = (int)seg.size() - 1;
+        while ((int)ckpt.size() > S - 1) { cudaFree(ckpt.back()); ckpt.pop_back(); }
+    }
+    // 1. forward pass, keeping psi after every segment but the last
+    bs_stats fwd{};
+    int rc = BS_OK;
+    // segments are queued back to back: the host plans segment j+1 while the GPU runs segment j
     cudaEventRecord(s->ev0, s->stream);
+    s->tc_events_used = 0;
+    s->defer_sync = true;
+    for (int j = 0; j < S && !rc; j++) {
+        rc = bs_evolve(s, ops + seg[(size_t)j], seg[(size_t)j + 1] - seg[(size_t)j], 0);
+        if (rc) break;
+        fwd.sweeps += s->stats.sweeps;
+        fwd.kernel_launches += s->stats.kernel_launches;
+        fwd.gates += s->stats.gates;
+        fwd.bytes_moved += s->stats.bytes_moved;
+        fwd.tc_gates += s->stats.tc_gates;
+        fwd.tc_launches += s->stats.tc_launches;
+        if (j + 1 < S) rc = bs_cuda_check(s, cudaMemcpyAsync(ckpt[(size_t)j], s->state, state_bytes, cudaMemcpyDeviceToDevice, s->stream), "checkpoint");
+    }
+    s->defer_sync = false;
+    if (rc) { cudaStreamSynchronize(s->stream); free_ckpt(); return rc; }
+    s->stats = fwd;
     // 2. lambda = H psi
     void* lam = nullptr;
     rc = bs_cuda_check(s, cudaMallocAsync(&lam, (size_t)len * esz, s->stream), "lambda allocation");
-    if (rc) return rc;
+    if (rc) { free_ckpt(); return rc; }
     std::vector<PauliTerm> terms((size_t)n_terms);
     for (int t = 0; t < n_terms; t++) {
         uint64_t x = xmask[t], z = zmask[t];
@@ -349,7 +416,7 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
         terms[(size_t)t].cl = (float)(coeffs[t] - (double)terms[(size_t)t].ch);
     }
     rc = bs_ensure_scratch(s, (int64_t)n_terms * (int64_t)sizeof(PauliTerm) + (int64_t)(n_params + 2) * 8 + 256);
-    if (rc) { cudaFreeAsync(lam, s->stream); return rc; }
+    if (rc) { cudaFreeAsync(lam, s->stream); free_ckpt(); return rc; }
     PauliTerm* d_terms = (PauliTerm*)s->scratch;
     double* d_acc = (double*)((char*)s->scratch + (((int64_t)n_terms * (int64_t)sizeof(PauliTerm) + 255) & ~255LL));
     cudaMemcpyAsync(d_terms, terms.data(), terms.size() * sizeof(PauliTerm), cudaMemcpyHostToDevice, s->stream);
@@ -366,15 +433,21 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
     }
     // 3. backward: reversed, daggered gate list with gradient markers before each parameterised gate
     std::vector<BwdItem> items;
+    std::vector<size_t> seg_item(1, 0);   // items of segment S-1-r start at seg_item[r]
+    int cur_seg = S - 1;
     for (int64_t i = n_ops - 1; i >= 0; i--) {
+        while (cur_seg > 0 && i < seg[(size_t)cur_seg]) {
+            cur_seg--;
+            seg_item.push_back(items.size());
+        }
         const bs_op& op = ops[i];
         if (op.kind != 0) continue;
         std::vector<HostGate> hg;
         rc = bs_lower_gate(s, op.matrix, op.n_targets, op.targets, op.n_controls, op.controls, op.control_values,
                            op.flags, false, hg);
-        if (rc) { cudaFreeAsync(lam, s->stream); return rc; }
+        if (rc) { cudaFreeAsync(lam, s->stream); free_ckpt(); return rc; }
         if (param_index[i] >= 0) {
-            if (param_index[i] >= n_params) { cudaFreeAsync(lam, s->stream); return bs_fail(s, BS_ERR_INVALID_ARG, "parameter index out of range"); }
+            if (param_index[i] >= n_params) { cudaFreeAsync(lam, s->stream); free_ckpt(); return bs_fail(s, BS_ERR_INVALID_ARG, "parameter index out of range"); }
             BwdItem m;
             m.marker = true;
             m.slot = param_index[i];
@@ -402,18 +475,22 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
             items.push_back(it);
         }
     }
-    // plan sweeps: markers need their flip bits in the tile, and they must not move
-    // past a gate sharing bits (they read the current psi and lambda)
+    while ((int)seg_item.size() < S) seg_item.push_back(items.size());
+    seg_item.push_back(items.size());
+    // plan sweeps segment by segment: markers need their flip bits in the tile, and they must not
+    // move past a gate sharing bits (they read the current psi and lambda)
     const int n_bits = n;
     const int T = std::min(BS_TILE_MAX_BITS, n_bits);
     const int L = std::min(BS_TILE_LOW_BITS, T);
     const int cap = T - L;
     std::vector<std::vector<int>> sweeps_items;
     std::vector<std::vector<int>> sweeps_hi;
-    {
-        const size_t G = items.size();
+    std::vector<int> sweep_restore;   // checkpoint to restore psi from before the sweep, -1 if none
+    for (int r = 0; r < S; r++) {
+        const size_t G = seg_item[(size_t)r + 1];
         std::vector<char> done(G, 0);
-        size_t remaining = G, first = 0;
+        size_t remaining = G - seg_item[(size_t)r], first = seg_item[(size_t)r];
+        bool seg_first = true;
         auto touch = [&](const BwdItem& it) {
             uint64_t m = it.g.cmask | it.zm | it.xm;
             for (int q = 0; q < it.g.k; q++) m |= 1ULL << it.g.ebit[q];
@@ -440,6 +517,7 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
                                (items[i].g.k > BS_TILE_MAXK || __builtin_popcountll(need(items[i])) > cap);
                 if (too_big || (items[i].marker && __builtin_popcountll(need(items[i])) > cap)) {
                     cudaFreeAsync(lam, s->stream);
+                    free_ckpt();
                     return bs_fail(s, BS_ERR_UNSUPPORTED, "adjoint gate too wide for a tile");
                 }
                 if (nch + add <= cap) {
@@ -459,6 +537,9 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
             std::sort(hi.begin(), hi.end());
             sweeps_items.push_back(idx);
             sweeps_hi.push_back(hi);
+            // entering segment S-1-r (r > 0): psi is its end state, kept by the forward pass
+            sweep_restore.push_back(seg_first && r > 0 ? S - 1 - r : -1);
+            seg_first = false;
         }
     }
     // pack device data
@@ -518,7 +599,7 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
     const int64_t b_m = al((int64_t)mats.size() * (int64_t)sizeof(float4));
     const int64_t b_p = al((int64_t)(perms.size() + 1) * 4);
     rc = bs_ensure_plan(s, b_ag + b_m + b_p);
-    if (rc) { cudaFreeAsync(lam, s->stream); return rc; }
+    if (rc) { cudaFreeAsync(lam, s->stream); free_ckpt(); return rc; }
     std::vector<char> host((size_t)(b_ag + b_m + b_p), 0);
     if (!ag.empty()) std::memcpy(host.data(), ag.data(), ag.size() * sizeof(AdjGate));
     if (!mats.empty()) std::memcpy(host.data() + b_ag, mats.data(), mats.size() * sizeof(float4));
@@ -533,6 +614,8 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
     cudaFuncSetAttribute(k_adjoint_sweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     const int64_t ntiles = (int64_t)1 << (n_bits - T);
     for (size_t sw = 0; sw < sweeps_items.size(); sw++) {
+        if (sweep_restore[sw] >= 0)
+            cudaMemcpyAsync(s->state, ckpt[(size_t)sweep_restore[sw]], state_bytes, cudaMemcpyDeviceToDevice, s->stream);
         SweepDesc d{};
         d.n_bits = n_bits;
         d.T = T;
@@ -561,10 +644,14 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
     cudaFreeAsync(lam, s->stream);
     cudaEventRecord(s->ev1, s->stream);
     rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "adjoint");
+    free_ckpt();
     if (rc) return rc;
     float ms = 0;
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);
-    s->stats.gpu_ms += ms;
+    s->stats.gpu_ms = ms;   // forward and backward
+    bs_collect_tc_time(s);
+    rc = bs_check_device_flag(s);
+    if (rc) return rc;
     *energy_out = res[(size_t)n_params];
     for (int p = 0; p < n_params; p++) grad_out[p] = res[(size_t)p];
     return BS_OK;

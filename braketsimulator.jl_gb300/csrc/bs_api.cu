@@ -218,6 +218,10 @@ int bs_set_tuning(bs_sim* s, int param, double value) {
             if (!reset && !(value < 1e9)) break;
             s->tune.tc_cost = reset ? -1.0 : value;
             return BS_OK;
+        case BS_TUNE_ADJ_SEGMENTS:
+            if (!reset && (iv < 1 || iv > 1024 || iv != value)) break;
+            s->tune.adj_segments = reset ? -1 : iv;
+            return BS_OK;
         default:
             return bs_fail(s, BS_ERR_INVALID_ARG, "unknown tuning parameter");
     }
@@ -232,6 +236,7 @@ int bs_get_tuning(bs_sim* s, int param, double* value) {
         case BS_TUNE_TC: *value = bs_tc_enabled(s) ? 1.0 : 0.0; return BS_OK;
         case BS_TUNE_TC_MIN_BITS: *value = bs_tc_min_bits(s); return BS_OK;
         case BS_TUNE_TC_COST: *value = bs_tc_cost(s); return BS_OK;
+        case BS_TUNE_ADJ_SEGMENTS: *value = s->tune.adj_segments; return BS_OK;
         default: return bs_fail(s, BS_ERR_INVALID_ARG, "unknown tuning parameter");
     }
 }
@@ -355,7 +360,7 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     if (!s) return BS_ERR_INVALID_ARG;
     if (n_ops < 0 || (n_ops > 0 && !ops)) return bs_fail(s, BS_ERR_INVALID_ARG, "bad op list");
     s->stats = bs_stats{};
-    s->tc_events_used = 0;
+    if (!s->defer_sync) s->tc_events_used = 0;   // deferred evolves keep their launch events for the caller
     s->alias_valid = false;
     if (!s->capturing) cudaEventRecord(s->ev0, s->stream);
     std::vector<HostGate> pending;
@@ -394,7 +399,7 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     }
     int rc = flush();
     if (rc) return rc;
-    if (s->capturing) return BS_OK;   // the graph's launcher synchronises and checks
+    if (s->capturing || s->defer_sync) return BS_OK;   // the graph's launcher / the caller synchronises and checks
     cudaEventRecord(s->ev1, s->stream);
     rc = bs_cuda_check(s, cudaEventSynchronize(s->ev1), "evolve");
     if (rc) return rc;

@@ -79,6 +79,7 @@ struct BsTuning {
     int tc = -1;             // fused tensor-core sweeps on (1) or off (0)
     int tc_min_bits = -1;    // vector bits from which fused tensor-core sweeps are used
     double tc_cost = -1;     // float-float cost (dense 1-qubit gates) above which a block is fused
+    int adj_segments = -1;   // adjoint gradients: forward segments (checkpoints + 1); -1 = from memory
 };
 
 struct bs_sim {
@@ -117,6 +118,7 @@ struct bs_sim {
     // buffer growth, and staging comes from an append-only pinned arena that lives as long as the
     // graph (the graph's copy nodes read it on every replay).
     bool capturing = false;
+    bool defer_sync = false;   // bs_evolve returns without synchronising (an internal caller syncs later)
     std::vector<std::pair<char*, size_t>> arena;   // chunks (pointer, capacity)
     size_t arena_used = 0;                          // bytes used in the last chunk
 };

@@ -221,12 +221,17 @@ int bs_batch_destroy(bs_batch* batch);
  *   BS_TUNE_TC            0|1     fused tensor-core sweeps (BS_TC)
  *   BS_TUNE_TC_MIN_BITS   n       vector bits from which they are used (BS_TC_MIN_BITS, 22)
  *   BS_TUNE_TC_COST       x       fuse a block when its float-float cost (dense 1-qubit gates)
- *                                 exceeds x (BS_TC_COST, 2) */
+ *                                 exceeds x (BS_TC_COST, 2)
+ *   BS_TUNE_ADJ_SEGMENTS  S >= 1  bs_adjoint_gradient: forward segments, psi kept after each of the
+ *                                 first S-1 (checkpoints); default (-1) from the parameterised gate
+ *                                 count and a quarter of the free memory, halved while allocation
+ *                                 fails; 1 = pure uncomputation */
 #define BS_TUNE_TILE_BITS     0
 #define BS_TUNE_TILE_THREADS  1
 #define BS_TUNE_TC            2
 #define BS_TUNE_TC_MIN_BITS   3
 #define BS_TUNE_TC_COST       4
+#define BS_TUNE_ADJ_SEGMENTS  5
 int bs_set_tuning(bs_sim* sim, int param, double value);
 int bs_get_tuning(bs_sim* sim, int param, double* value);
 /* n settings (params[i] = values[i]) on every handle of a captured batch, then one rebuild of its

@@ -75,3 +75,70 @@ def test_adjoint_complex64_state(n):
     scale = max(1.0, sum(abs(c) for c, _ in h))
     assert abs(e64 - e128) < 2e-5 * scale
     assert np.max(np.abs(g64 - g128)) < 2e-5 * scale
+
+
+@pytest.mark.parametrize("segments", [1, 2, 5, 40])
+def test_adjoint_checkpoint_segments(segments):
+    """Forward checkpoints (psi kept after each segment, restored on the way back) give the same
+    gradients as pure uncomputation, for any segment count (including more segments than gates
+    per segment allow)."""
+    n = 9
+    rng = np.random.default_rng(77)
+    ops = ansatz(n, 3, rng)
+    h = hamiltonian(n, 8, rng)
+    ref = bs.StateVectorSimulator(n, 0)
+    bs.set_tuning(ref, adj_segments=1)
+    e1, g1 = adj.adjoint_gradient(ref, ops, h)
+    sim = bs.StateVectorSimulator(n, 0)
+    bs.set_tuning(sim, adj_segments=segments)
+    e, g = adj.adjoint_gradient(sim, ops, h)
+    assert abs(e - e1) < 1e-12
+    assert np.max(np.abs(g - g1)) < 1e-12
+    ps = adj.parameter_shift_gradient(sim, ops, h)
+    assert np.max(np.abs(g - ps)) < 1e-10
+
+
+def test_adjoint_checkpoints_bound_complex64_drift():
+    """complex64: uncomputing psi through a deep circuit drifts; checkpoints reset it per segment."""
+    n = 10
+    rng = np.random.default_rng(90)
+    ops = ansatz(n, 12, rng)
+    h = hamiltonian(n, 10, rng)
+    _, g128 = adj.adjoint_gradient(bs.StateVectorSimulator(n, 0), ops, h)
+    errs = {}
+    for seg in (1, 16):
+        sim = bs.StateVectorSimulator(n, 0, precision="c64")
+        bs.set_tuning(sim, adj_segments=seg)
+        _, g64 = adj.adjoint_gradient(sim, ops, h)
+        errs[seg] = float(np.max(np.abs(g64 - g128)))
+    scale = max(1.0, sum(abs(c) for c, _ in h))
+    assert errs[16] < 2e-5 * scale
+    assert errs[16] <= errs[1] * 1.5
+
+
+def test_rrule_and_torch_autograd():
+    import torch
+    n = 6
+    rng = np.random.default_rng(12)
+    h = hamiltonian(n, 6, rng)
+    theta0 = rng.uniform(-np.pi, np.pi, size=3 * n)
+
+    def build(th):
+        ops = []
+        for q in range(n):
+            ops.append(bs.Instruction(bs.Ry(float(th[q])), [q]))
+            ops.append(bs.Instruction(bs.Rz(float(th[n + q])), [q]))
+        for q in range(n):
+            ops.append(bs.Instruction(bs.ZZ(float(th[2 * n + q])), [q, (q + 1) % n]))
+        return ops
+
+    sim = bs.StateVectorSimulator(n, 0)
+    e, pb = bs.energy_rrule(sim, build(theta0), h)
+    ps = adj.parameter_shift_gradient(sim, build(theta0), h)
+    assert np.max(np.abs(pb(2.0) - 2.0 * ps)) < 1e-10
+    f = bs.torch_energy(build, h, sim)
+    theta = torch.tensor(theta0, dtype=torch.float64, requires_grad=True)
+    out = 3.0 * f(theta)
+    out.backward()
+    assert abs(out.item() - 3.0 * e) < 1e-12
+    assert np.max(np.abs(theta.grad.numpy() - 3.0 * ps)) < 1e-10

@@ -13,7 +13,10 @@ AT = __import__("braketsimulator_gb300.autotune", fromlist=["candidates"])
 def test_tuning_round_trip_and_validation():
     sim = bs.StateVectorSimulator(14, 0)
     bs.set_tuning(sim, tile_bits=11, tile_threads=512, tc=0, tc_min_bits=18, tc_cost=3.5)
-    assert bs.get_tuning(sim) == {"tile_bits": 11, "tile_threads": 512, "tc": 0, "tc_min_bits": 18, "tc_cost": 3.5}
+    assert bs.get_tuning(sim) == {"tile_bits": 11, "tile_threads": 512, "tc": 0, "tc_min_bits": 18, "tc_cost": 3.5,
+                                  "adj_segments": -1}
+    bs.set_tuning(sim, adj_segments=4)
+    assert bs.get_tuning(sim)["adj_segments"] == 4
     bs.set_tuning(sim, tile_bits=None, tile_threads=None, tc=None, tc_min_bits=None, tc_cost=None)
     t = bs.get_tuning(sim)
     assert t["tile_bits"] == 12 and t["tile_threads"] in (256, 512)
