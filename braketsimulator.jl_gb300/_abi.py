@@ -102,6 +102,7 @@ SIGNATURES = {
     "bs_batch_set_tuning": (_i32, [_p, _i32, _P(_i32), _P(_f64)]),
     "bs_set_tuning": (_i32, [_p, _i32, _f64]),
     "bs_get_tuning": (_i32, [_p, _i32, _P(_f64)]),
+    "bs_reduced_density_matrix": (_i32, [_p, _i32, _P(_i32), _P(_f64)]),
     "bs_synchronize": (_i32, [_p]),
     "bs_state_device_ptr": (_i32, [_p, _P(_p)]),
 }

@@ -88,10 +88,21 @@ def permute_density_matrix(rho: np.ndarray, qubit_count: int, targets) -> np.nda
     return out
 
 
+def _jshl(x, k):
+    """Julia's x << k: a negative count shifts the other way."""
+    return x << k if k >= 0 else x >> -k
+
+
 def _swap_bits(ix, mapping):
+    """swap_bits (src/dm_simulator.jl:264-278), with Julia's shift semantics: a mapping entry whose
+    source bit is negative (unsorted targets numbered beyond the output size) reads as 0 and flips
+    only the other bit."""
     for a, b in mapping.items():
-        if a < b and ((ix >> a) & 1) != ((ix >> b) & 1):
-            ix ^= (1 << a) | (1 << b)
+        if a < b:
+            av = _jshl(_jshl(1, a) & ix, -a)
+            bv = _jshl(_jshl(1, b) & ix, -b)
+            if av != bv:
+                ix ^= _jshl(1, a) ^ _jshl(1, b)
     return ix
 
 
@@ -140,6 +151,34 @@ def partial_trace(state, output_qubits=None):
             else:
                 out[oi, oj] = np.sum(state[fi, fj])
     return out
+
+
+def reduced_density_matrix(sim, output_qubits):
+    """partial_trace of the simulator's state keeping output_qubits (any order), computed on the
+    device; the final reordering of unsorted targets follows ``partial_trace`` above."""
+    output_qubits = list(output_qubits)
+    out = sim.reduced_density_matrix(output_qubits)
+    if output_qubits == sorted(output_qubits):
+        return out
+    fn = len(output_qubits)
+    mapping = dict(zip([fn - q - 1 for q in output_qubits], [fn - q - 1 for q in range(fn)]))
+    dim = out.shape[0]
+    perm = np.array([_swap_bits(ix, mapping) for ix in range(dim)], dtype=np.int64)
+    res = np.zeros_like(out)
+    if isinstance(sim, DensityMatrixSimulator):
+        # the reference assigns entry by entry in row-major order: the last write to a cell wins
+        tgt = (perm[:, None] * dim + perm[None, :]).ravel()[::-1]
+        _, first = np.unique(tgt, return_index=True)
+        src = out.ravel()[::-1][first]
+        res.ravel()[tgt[first]] = src
+    else:
+        # the reference accumulates over ix <= jx and mirrors the conjugate off the diagonal
+        iu, ju = np.triu_indices(dim)
+        oi, oj = perm[iu], perm[ju]
+        np.add.at(res, (oi, oj), out[iu, ju])
+        off = oi != oj
+        np.add.at(res, (oj[off], oi[off]), np.conj(out[iu, ju][off]))
+    return res
 
 
 def _targets(rt, sim):
@@ -194,5 +233,7 @@ def calculate(rt, sim):
             return rho if full else sim.density_matrix()
         if len(t) == n:
             return permute_density_matrix(rho if full else sim.density_matrix(), n, list(t))
+        if 1 <= len(set(t)) <= 12 and len(set(t)) < n:
+            return reduced_density_matrix(sim, list(t))
         return partial_trace(rho if full else sim.state_vector, list(t))
     raise TypeError(f"unsupported result type {rt!r}")

@@ -271,6 +271,15 @@ class AbstractSimulator:
         self._h.call("bs_sample_direct", _abi.dptr(u), u.size, float(wsum), _abi.i64ptr(out))
         return out
 
+    def reduced_density_matrix(self, qubits) -> np.ndarray:
+        """Partial trace keeping ``qubits`` (1..12 of them), on the device; row/column index bit r
+        belongs to the r-th highest-numbered kept qubit (the reference's loop order)."""
+        q = np.ascontiguousarray(list(qubits), dtype=np.int32)
+        d = 1 << q.size
+        out = np.empty(2 * d * d, dtype=np.float64)
+        self._h.call("bs_reduced_density_matrix", int(q.size), _abi.iptr(q), _abi.dptr(out))
+        return out.view(np.complex128).reshape(d, d)
+
     def marginal_probabilities(self, targets) -> np.ndarray:
         t = np.ascontiguousarray(targets, dtype=np.int32)
         out = np.empty(1 << t.size, dtype=np.float64)

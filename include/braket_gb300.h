@@ -186,6 +186,13 @@ int bs_expectation_pauli_noalloc(const void* state_dev, int kind, int n_qubits, 
                                  const uint64_t* xmask, const uint64_t* zmask, const double* coeffs,
                                  double* out, void* stream);
 
+/* ---- reduced density matrix: partial_trace (src/sv_simulator.jl:273-318, src/dm_simulator.jl:280-323)
+ * for the DensityMatrix result type (src/result_types.jl:239-246), computed on the device.
+ * Keeps the n_keep (1..12) given qubits, traces out the rest; out = 2^k x 2^k complex128,
+ * row-major, interleaved, with output index bit r <-> the r-th smallest kept endian bit (the
+ * reference's loop order before its own final permutation of unsorted targets). */
+int bs_reduced_density_matrix(bs_sim* sim, int n_keep, const int* qubits, double* out);
+
 /* ---- batched simulate (src/BraketSimulator.jl:347-395): n_circuits independent circuits, each
  * from |0...0> on n_qubits[c] qubits with ops[c][0..n_ops[c]).  Returns per circuit n_terms Pauli
  * expectations (term t of circuit c at xmask/zmask[c*n_terms + t], bit q <-> qubit q) and `shots`

@@ -185,3 +185,44 @@ def test_simulate_program_ghz_batch():
         m = r["measurements"]
         assert m.shape == (1000, 5)
         assert 400 < np.sum(np.all(m == 0, axis=1)) < 600 and 400 < np.sum(np.all(m == 1, axis=1)) < 600
+
+
+@pytest.mark.parametrize("n,keep", [(5, (3,)), (5, (0, 2, 1)), (9, (8, 0, 4, 2)), (11, (1, 3, 5, 7, 9, 10)),
+                                    (13, tuple(range(0, 13, 2))), (14, tuple(range(2, 14)))])
+def test_device_partial_trace_matches_host(n, keep):
+    """The device partial trace (float-float sums) equals the host restatement of the reference's
+    loops, for state vectors and density matrices, sorted and unsorted kept qubits."""
+    rng = np.random.default_rng(n + len(keep))
+    ops = random_circuit(n, 40, rng)
+    sv = bs.StateVectorSimulator(n, 0)
+    sv.evolve(ops)
+    psi = sv.state_vector
+    got = bs.calculate(bs.DensityMatrix(keep), sv)
+    if len(keep) <= 8:
+        ref = bs.partial_trace(psi, list(keep))   # the reference's loops, restated
+    else:
+        # many kept qubits: the same matrix by tensor contraction (kept qubits in descending order of
+        # their endian bits, i.e. ascending qubit numbers, then the reference's reordering)
+        t = psi.reshape([2] * n)
+        kept = sorted(keep)
+        tr = [q for q in range(n) if q not in kept]
+        a = np.transpose(t, kept + tr).reshape(1 << len(kept), -1)
+        nat = a @ a.conj().T
+        ref = nat if list(keep) == kept else None
+    if ref is not None:
+        assert np.max(np.abs(got - ref)) < 1e-13
+    if n <= 7:
+        dm = bs.DensityMatrixSimulator(n, 0)
+        dm.evolve(ops + [bs.Instruction(bs.Depolarizing(0.1), [0])])
+        rho = dm.density_matrix
+        assert np.max(np.abs(bs.calculate(bs.DensityMatrix(keep), dm) - bs.partial_trace(rho, list(keep)))) < 1e-13
+
+
+def test_device_partial_trace_complex64():
+    n = 12
+    rng = np.random.default_rng(3)
+    ops = random_circuit(n, 60, rng)
+    s64 = bs.StateVectorSimulator(n, 0, precision="c64")
+    s64.evolve(ops)
+    ref = bs.partial_trace(oracle.OracleSV(n).evolve(ops).psi, [2, 7, 11])
+    assert np.max(np.abs(s64.reduced_density_matrix([2, 7, 11]) - ref)) < 1e-5
