@@ -59,32 +59,34 @@ def marginal_probability(probs: np.ndarray, qubit_count: int, targets) -> np.nda
     return np.ascontiguousarray(m).reshape(-1) if kept else np.array([float(np.sum(p))])
 
 
-def permute_probability(probs: np.ndarray, qubit_count: int, targets) -> np.ndarray:
-    """src/result_types.jl:115-127."""
+def _permuted_indices(qubit_count: int, targets) -> np.ndarray:
+    """new index of every ix (vectorised): bit q of new = bit (qubit_count - targets[q] - 1) of ix."""
     t = list(targets)
-    out = np.zeros(1 << len(t))
-    for ix in range(1 << len(t)):
-        bits = [(ix >> q) & 1 for q in range(qubit_count)]
-        perm = [bits[qubit_count - tt - 1] for tt in t]
-        new = sum(b << q for q, b in zip(range(qubit_count), perm))
-        out[new] = probs[ix]
+    ix = np.arange(1 << len(t), dtype=np.int64)
+    new = np.zeros_like(ix)
+    for q, tt in enumerate(t[:qubit_count]):
+        new |= ((ix >> (qubit_count - tt - 1)) & 1) << q
+    return new
+
+
+def permute_probability(probs: np.ndarray, qubit_count: int, targets) -> np.ndarray:
+    """src/result_types.jl:115-127 (assignment in ascending ix: the last write to a slot wins)."""
+    new = _permuted_indices(qubit_count, targets)
+    out = np.zeros(new.size)
+    rev = new[::-1]
+    _, first = np.unique(rev, return_index=True)
+    out[rev[first]] = np.asarray(probs)[: new.size][::-1][first]
     return out
 
 
 def permute_density_matrix(rho: np.ndarray, qubit_count: int, targets) -> np.ndarray:
-    """src/result_types.jl:129-149."""
-    t = list(targets)
-    d = 1 << len(t)
-
-    def idx(ix):
-        bits = [(ix >> q) & 1 for q in range(qubit_count)]
-        perm = [bits[qubit_count - tt - 1] for tt in t]
-        return sum(b << q for q, b in zip(range(qubit_count), perm))
-
+    """src/result_types.jl:129-149 (assignment in row-major order: the last write wins)."""
+    new = _permuted_indices(qubit_count, targets)
+    d = new.size
     out = np.zeros((d, d), dtype=rho.dtype)
-    for ix in range(d):
-        for jx in range(d):
-            out[idx(ix), idx(jx)] = rho[ix, jx]
+    tgt = (new[:, None] * d + new[None, :]).ravel()[::-1]
+    _, first = np.unique(tgt, return_index=True)
+    out.ravel()[tgt[first]] = np.asarray(rho)[:d, :d].ravel()[::-1][first]
     return out
 
 
