@@ -122,8 +122,19 @@ __device__ __forceinline__ void st4(uint32_t taddr, const uint32_t (&w)[4]) {
                  "r"(w[2]), "r"(w[3])
                  : "memory");
 }
+// no memory clobber: TMEM stores stay ordered against the other tcgen05 asm (all volatile), and
+// shared-memory loads of the slicing may be scheduled across them
 __device__ __forceinline__ void st2(uint32_t taddr, uint32_t w0, uint32_t w1) {
-    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1,%2};" ::"r"(taddr), "r"(w0), "r"(w1) : "memory");
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1,%2};" ::"r"(taddr), "r"(w0), "r"(w1));
+}
+// wait for this thread's TMEM loads; the registers they fill are tied to the wait so that no use of
+// them is scheduled before it
+__device__ __forceinline__ void wait_ld16(uint32_t (&r)[8], uint32_t (&q)[8]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(q[0]), "+r"(q[1]), "+r"(q[2]), "+r"(q[3]), "+r"(q[4]), "+r"(q[5]), "+r"(q[6]), "+r"(q[7])
+                 :
+                 : "memory");
 }
 __device__ __forceinline__ void ld8(uint32_t taddr, uint32_t (&r)[8]) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -333,14 +344,18 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
     const float osc = __uint_as_float((uint32_t)(ebc - 13 + g.tc_eu) << 23);       // 2^(E + eu - 14)
     const uint32_t lane = (uint32_t)((warp & 3) * 32) << 16;
     const f2 sc2 = pk(sc, sc);
+    // all of the thread's amplitudes loaded first (the loads overlap), then split and stored
+    float4 vv[NA];
+#pragma unroll
+    for (int a = 0; a < NA; a++) vv[a] = sm[spm ^ tsw[a]];
 #pragma unroll
     for (int c = 0; c < NA / 2; c++) {
         uint32_t w[6][2];
 #pragma unroll
         for (int a = 0; a < 2; a++) {
-            const float4 vv = sm[spm ^ tsw[2 * c + a]];
+            const float4 v = vv[2 * c + a];
             f2 q[6];
-            digits2(mul2(pk(vv.x, vv.y), sc2), mul2(pk(vv.z, vv.w), sc2), q);
+            digits2(mul2(pk(v.x, v.y), sc2), mul2(pk(v.z, v.w), sc2), q);
 #pragma unroll
             for (int j = 0; j < 6; j++) {
                 const float2 d = up(q[j]);
@@ -384,19 +399,22 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
         fence_after();
         if (k == 0 && tid == 0) issue_round<3>(st.tmem, kD1, b0, st.bar + 16u);
 #pragma unroll
-        for (int c = 0; c < NA / 4; c++) {
-            uint32_t r[8];
-            ld8(st.tmem + lane + dcol + (uint32_t)(2 * NA * h + 8 * c), r);
-            wait_ld();
+        for (int c2 = 0; c2 < NA / 4; c2 += 2) {   // two 8-column loads in flight, one wait
+            uint32_t r[2][8];
+            ld8(st.tmem + lane + dcol + (uint32_t)(2 * NA * h + 8 * c2), r[0]);
+            ld8(st.tmem + lane + dcol + (uint32_t)(2 * NA * h + 8 * c2 + 8), r[1]);
+            wait_ld16(r[0], r[1]);
 #pragma unroll
-            for (int p = 0; p < 4; p++) {
-                const int o = 4 * c + p;
-                const f2 gv = pk(__uint_as_float(r[2 * p]), __uint_as_float(r[2 * p + 1]));
-                if (k == 0) E[o] = gv;
-                else if (k == 1) E[o] = add2(E[o], gv);
-                else if (k == 2) S[o] = gv;
-                else E[o] = add2(E[o], two_sum2(S[o], gv));
-            }
+            for (int u = 0; u < 2; u++)
+#pragma unroll
+                for (int p = 0; p < 4; p++) {
+                    const int o = 4 * (c2 + u) + p;
+                    const f2 gv = pk(__uint_as_float(r[u][2 * p]), __uint_as_float(r[u][2 * p + 1]));
+                    if (k == 0) E[o] = gv;
+                    else if (k == 1) E[o] = add2(E[o], gv);
+                    else if (k == 2) S[o] = gv;
+                    else E[o] = add2(E[o], two_sum2(S[o], gv));
+                }
         }
         fence_before();
         __syncwarp();
