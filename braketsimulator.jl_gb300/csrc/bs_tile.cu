@@ -130,8 +130,11 @@ __device__ void tile_monomial(float4* sm, int T, const TileGate& g, const int32_
         }
 #pragma unroll
         for (int c = 0; c < D; c++) {
-            int r = __ldg(p + 2 * c), ph = __ldg(p + 2 * c + 1);
-            sm[idx[r]] = c4f(cmul_ipow(f4c(x[c]), ph));
+            const int r = __ldg(p + 2 * c), ph = __ldg(p + 2 * c + 1);
+            int j = jb;
+#pragma unroll
+            for (int q = 0; q < K; q++) if ((r >> q) & 1) j |= 1 << g.tbit[q];
+            sm[sx<SW>(j)] = c4f(cmul_ipow(f4c(x[c]), ph));
         }
     }
 }
@@ -150,12 +153,29 @@ __device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const flo
                           int64_t base, OT off_tab, int osh) {
     const int nt = 1 << T, lowmask = (1 << L) - 1;
     const float4* m = mats + g.mat_off;
+    // pattern bit q: tile bit tbit[q] (32-bit), or a CTA constant for a bit outside the tile;
+    // gates with more than BS_TILE_MAXK bits take the pattern from the 64-bit global index
+    const bool fast = g.k <= BS_TILE_MAXK;
+    int cst = 0, nk = 0;
+    uint32_t enc = 0;   // per in-tile pattern bit: tile position (5 bits) | q << 5, one byte each
+    if (fast)
+        for (int q = 0; q < g.k; q++) {
+            if (g.tbit[q] >= 0) enc |= (uint32_t)(g.tbit[q] | (q << 5)) << (8 * nk++);
+            else cst |= (int)((base >> g.gbit[q]) & 1) << q;
+        }
     for (int j = threadIdx.x; j < nt; j += blockDim.x) {
         if ((j & (int)g.lc_mask) != (int)g.lc_val) continue;
-        int64_t gi = base | ((int64_t)off_tab[j >> L] << osh) | (int64_t)(j & lowmask);
         const int js = sx<SW>(j);
-        int di = 0;
-        for (int q = 0; q < g.k; q++) di |= (int)((gi >> g.gbit[q]) & 1) << q;
+        int di = cst;
+        if (fast) {
+            for (int u = 0; u < nk; u++) {
+                const uint32_t b = (enc >> (8 * u)) & 255u;
+                di |= ((j >> (b & 31u)) & 1) << (b >> 5);
+            }
+        } else {
+            const int64_t gi = base | ((int64_t)off_tab[j >> L] << osh) | (int64_t)(j & lowmask);
+            for (int q = 0; q < g.k; q++) di |= (int)((gi >> g.gbit[q]) & 1) << q;
+        }
         float4 d = __ldg(m + di);
         if (d.y == 0.f && d.w == 0.f) {
             if (d.z == 0.f && d.x == 1.f) continue;
@@ -558,6 +578,17 @@ __device__ void tile_dense_c64(float2* sm, int T, const TileGate& g, const float
     const int ngroups = 1 << (T - K);
     const float4* m = mats + g.mat_off;
     const uint32_t lcm = g.lc_mask, lcv = g.lc_val;
+    // 1- and 2-target matrices are held in registers across the thread's groups
+    constexpr int MR = K <= 2 ? D * D : 1;
+    float mre[MR], mim[MR];
+    if (K <= 2) {
+#pragma unroll
+        for (int e = 0; e < MR; e++) {
+            const float4 mv = __ldg(m + e);
+            mre[e] = mv.x;
+            mim[e] = mv.z;
+        }
+    }
     for (int gr = threadIdx.x; gr < ngroups; gr += blockDim.x) {
         int jb = gr;
 #pragma unroll
@@ -578,9 +609,11 @@ __device__ void tile_dense_c64(float2* sm, int T, const TileGate& g, const float
             float re = 0.f, im = 0.f;
 #pragma unroll
             for (int c = 0; c < D; c++) {
-                const float4 mv = __ldg(m + r * D + c);
-                re = fmaf(mv.x, x[c].x, fmaf(-mv.z, x[c].y, re));
-                im = fmaf(mv.x, x[c].y, fmaf(mv.z, x[c].x, im));
+                float ar, ai;
+                if (K <= 2) { ar = mre[(r * D + c) % MR]; ai = mim[(r * D + c) % MR]; }
+                else { const float4 mv = __ldg(m + r * D + c); ar = mv.x; ai = mv.z; }
+                re = fmaf(ar, x[c].x, fmaf(-ai, x[c].y, re));
+                im = fmaf(ar, x[c].y, fmaf(ai, x[c].x, im));
             }
             sm[idx[r]] = make_float2(re, im);
         }
@@ -615,7 +648,13 @@ __device__ void tile_mono_c64(float2* sm, int T, const TileGate& g, const int32_
             x[c] = sm[j];
         }
 #pragma unroll
-        for (int c = 0; c < D; c++) sm[idx[__ldg(p + 2 * c)]] = c64_ipow(x[c], __ldg(p + 2 * c + 1));
+        for (int c = 0; c < D; c++) {
+            const int r = __ldg(p + 2 * c);
+            int j = jb;
+#pragma unroll
+            for (int q = 0; q < K; q++) if ((r >> q) & 1) j |= 1 << tb[q];
+            sm[j] = c64_ipow(x[c], __ldg(p + 2 * c + 1));
+        }
     }
 }
 
@@ -623,6 +662,27 @@ __device__ void tile_diag_c64(float2* sm, int T, int L, const TileGate& g, const
                               const int64_t* off_tab) {
     const int nt = 1 << T, lowmask = (1 << L) - 1;
     const float4* m = mats + g.mat_off;
+    if (g.k <= BS_TILE_MAXK) {
+        // bit q of the pattern: tile bit tbit[q], or a constant of the CTA when the bit is outside the tile
+        int cst = 0, nk = 0;
+        uint32_t enc = 0;   // per in-tile pattern bit: tile position (5 bits) | q << 5, one byte each
+        for (int q = 0; q < g.k; q++) {
+            if (g.tbit[q] >= 0) enc |= (uint32_t)(g.tbit[q] | (q << 5)) << (8 * nk++);
+            else cst |= (int)((base >> g.gbit[q]) & 1) << q;
+        }
+        for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+            if ((j & (int)g.lc_mask) != (int)g.lc_val) continue;
+            int di = cst;
+            for (int u = 0; u < nk; u++) {
+                const uint32_t b = (enc >> (8 * u)) & 255u;
+                di |= ((j >> (b & 31u)) & 1) << (b >> 5);
+            }
+            const float4 d = __ldg(m + di);
+            if (d.z == 0.f && d.x == 1.f && d.y == 0.f) continue;
+            sm[j] = c64_mul(d, sm[j]);
+        }
+        return;
+    }
     for (int j = threadIdx.x; j < nt; j += blockDim.x) {
         if ((j & (int)g.lc_mask) != (int)g.lc_val) continue;
         const int64_t gi = base | off_tab[j >> L] | (int64_t)(j & lowmask);
