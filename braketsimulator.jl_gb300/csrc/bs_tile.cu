@@ -30,6 +30,18 @@ __device__ __forceinline__ int sx(int j) { return SW ? tc::sw(j) : j; }
 // Tile amplitudes in shared memory are float4 (re hi, im hi, re lo, im lo): the two high words and
 // the two low words each form an aligned register pair for the packed f32x2 arithmetic of the
 // tensor-core sweep.  Matrix entries in global memory are float4 (re hi, re lo, im hi, im lo).
+// Gate descriptors of a sweep are staged in shared memory in chunks (one coalesced copy per chunk
+// instead of dependent global loads of every field by every thread at every gate).
+constexpr int kGateChunk = 32;
+__device__ __forceinline__ void stage_gates(TileGate* dst, const TileGate* __restrict__ src, int ng) {
+    __syncthreads();   // the previous chunk is no longer read
+    const int words = ng * (int)(sizeof(TileGate) / 4);
+    const int* s = reinterpret_cast<const int*>(src);
+    int* t = reinterpret_cast<int*>(dst);
+    for (int w = threadIdx.x; w < words; w += blockDim.x) t[w] = __ldg(s + w);
+    __syncthreads();
+}
+
 __device__ __forceinline__ cff f4c(float4 v) { return {v.x, v.z, v.y, v.w}; }
 __device__ __forceinline__ float4 c4f(const cff& c) { return make_float4(c.rh, c.ih, c.rl, c.il); }
 __device__ __forceinline__ cff f4m(float4 v) { return {v.x, v.y, v.z, v.w}; }
@@ -289,8 +301,12 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
         smem[j] = c4f(load_c128(__ldcs(psi + gidx)));
     }
     __syncthreads();
-    for (int gi = 0; gi < d.n_gates; gi++) {
-        const TileGate& g = d.gates[gi];
+    __shared__ TileGate s_gates[kGateChunk];
+    for (int g0 = 0; g0 < d.n_gates; g0 += kGateChunk) {
+    const int ng = min(kGateChunk, d.n_gates - g0);
+    stage_gates(s_gates, d.gates + g0, ng);
+    for (int gl = 0; gl < ng; gl++) {
+        const TileGate& g = s_gates[gl];
         if ((base & (int64_t)g.gc_mask) != (int64_t)g.gc_val) continue;   // uniform in the CTA
         const int kind = g.kind, k = g.k;
         if (kind == 3) {
@@ -315,6 +331,7 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
             else if (KMAX > 2) tile_monomial<4>(smem, T, g, d.perms);
         }
         __syncthreads();
+    }
     }
     for (int j = threadIdx.x; j < nt; j += blockDim.x) {
         int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
@@ -695,7 +712,7 @@ __device__ void tile_diag_c64(float2* sm, int T, int L, const TileGate& g, const
 }
 
 template <int KMAX>
-__global__ void __launch_bounds__(kThreads) k_tile_sweep_c64(float2* __restrict__ psi, SweepDesc d, int64_t tile0) {
+__global__ void __launch_bounds__(kThreads, KMAX == 2 ? 4 : 3) k_tile_sweep_c64(float2* __restrict__ psi, SweepDesc d, int64_t tile0) {
     extern __shared__ float4 smem4[];
     float2* smem = reinterpret_cast<float2*>(smem4);
     const int T = d.T, L = d.L, H = T - L;
@@ -721,8 +738,12 @@ __global__ void __launch_bounds__(kThreads) k_tile_sweep_c64(float2* __restrict_
     for (int j = threadIdx.x; j < nt; j += blockDim.x)
         smem[j] = __ldcs(psi + (base | off_tab[j >> L] | (int64_t)(j & lowmask)));
     __syncthreads();
-    for (int gi = 0; gi < d.n_gates; gi++) {
-        const TileGate& g = d.gates[gi];
+    __shared__ TileGate s_gates[kGateChunk];
+    for (int g0 = 0; g0 < d.n_gates; g0 += kGateChunk) {
+    const int ng = min(kGateChunk, d.n_gates - g0);
+    stage_gates(s_gates, d.gates + g0, ng);
+    for (int gl = 0; gl < ng; gl++) {
+        const TileGate& g = s_gates[gl];
         if ((base & (int64_t)g.gc_mask) != (int64_t)g.gc_val) continue;
         const int kind = g.kind, k = g.k;
         if (kind == 3) {
@@ -744,6 +765,7 @@ __global__ void __launch_bounds__(kThreads) k_tile_sweep_c64(float2* __restrict_
             else if (KMAX > 2) tile_mono_c64<4>(smem, T, g, d.perms);
         }
         __syncthreads();
+    }
     }
     for (int j = threadIdx.x; j < nt; j += blockDim.x)
         __stcs(psi + (base | off_tab[j >> L] | (int64_t)(j & lowmask)), smem[j]);
