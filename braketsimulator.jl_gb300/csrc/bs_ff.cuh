@@ -126,6 +126,34 @@ __device__ __forceinline__ ff acc_done(const ffacc& a) {
     return {s, __fsub_rn(a.c, __fsub_rn(s, a.s))};
 }
 
+// Two FP32 values in one aligned register pair (low half first), for the packed f32x2 instructions:
+// one issue slot per pair instead of two, the same rounding (round to nearest even) per half.
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 up(f2 v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
 // complex MAC into two accumulators: (ar, ai) += m * x, m = (mrh+mrl) + i(mih+mil)
 __device__ __forceinline__ void cmac_first(ffacc& ar, ffacc& ai, const cff& m, const cff& x) {
     acc_first(ar, m.rh, m.rl, x.rh, x.rl);

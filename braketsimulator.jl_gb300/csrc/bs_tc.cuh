@@ -180,34 +180,6 @@ __device__ __forceinline__ float two_sum(float& s, float g) {
     return e;
 }
 
-// Two FP32 values in one aligned register pair (low half first), for the packed f32x2 instructions:
-// one issue slot per pair instead of two, the same rounding (round to nearest even) per half.
-typedef unsigned long long f2;
-__device__ __forceinline__ f2 pk(float a, float b) {
-    f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ float2 up(f2 v) {
-    float2 r;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
-    return r;
-}
-__device__ __forceinline__ f2 add2(f2 a, f2 b) {
-    f2 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
-    f2 d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
-    f2 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
 // digits() on both halves
 __device__ __forceinline__ void digits2(f2 yh, f2 yl, f2 (&q)[6]) {
     const f2 c0 = pk(12582912.0f, 12582912.0f), c1 = pk(49152.0f, 49152.0f), c2 = pk(192.0f, 192.0f),
