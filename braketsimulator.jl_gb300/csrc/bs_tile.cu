@@ -10,6 +10,7 @@
 // src/dm_simulator.jl:130-140 is two tile gates (column bits U, row bits conj U).
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstring>
 #include <thread>
 #include "bs_internal.h"
@@ -1125,6 +1126,101 @@ inline float4 to_cff(double re, double im) {
 
 }  // namespace
 
+namespace {
+
+bool plain_cz(const HostGate& h) {
+    return h.kind == 1 && h.k == 1 && h.mat.size() == 4 && h.mat[0] == 1.0 && h.mat[1] == 0.0 && h.mat[2] == -1.0 &&
+           h.mat[3] == 0.0 && __builtin_popcountll(h.cmask) == 1 && h.cval == h.cmask;
+}
+
+uint64_t gate_bits(const HostGate& h) {
+    uint64_t m = h.cmask;
+    if (h.kind == 5) return ~0ULL;
+    for (int q = 0; q < h.k; q++) m |= 1ULL << h.ebit[q];
+    return m;
+}
+
+// Diagonal gates (other than CZ, which merge into parity phases when packed) are folded into one
+// diagonal table over the union of their bits, up to kMaxMergedDiag bits.  The open table floats
+// forward past gates it commutes with (diagonal ones, and any gate on other bits), and is emitted
+// before the first non-diagonal gate that touches one of its bits.  One pass over the tile then
+// replaces a pass per gate.
+constexpr int kMaxMergedDiag = BS_TILE_MAXK;
+
+struct DiagTable {
+    uint64_t bits = 0;                 // endian bits, ascending in ebit order
+    std::vector<int> eb;
+    std::vector<std::complex<double>> d;
+};
+
+void diag_absorb(DiagTable& t, const HostGate& h) {
+    const uint64_t nb = t.bits | gate_bits(h);
+    std::vector<int> eb;
+    for (int e = 0; e < 64; e++) if ((nb >> e) & 1ULL) eb.push_back(e);
+    const int k = (int)eb.size();
+    std::vector<std::complex<double>> d((size_t)1 << k);
+    for (int x = 0; x < (1 << k); x++) {
+        uint64_t g = 0;   // the assignment x on the endian bits
+        for (int q = 0; q < k; q++) if ((x >> q) & 1) g |= 1ULL << eb[(size_t)q];
+        std::complex<double> v(1.0, 0.0);
+        if (!t.eb.empty() || t.bits == 0) {
+            int xi = 0;
+            for (size_t q = 0; q < t.eb.size(); q++) xi |= (int)((g >> t.eb[q]) & 1ULL) << q;
+            if (!t.d.empty()) v = t.d[(size_t)xi];
+        }
+        if ((g & h.cmask) == h.cval) {
+            int hi = 0;
+            for (int q = 0; q < h.k; q++) hi |= (int)((g >> h.ebit[q]) & 1ULL) << q;
+            v *= std::complex<double>(h.mat[2 * hi], h.mat[2 * hi + 1]);
+        }
+        d[(size_t)x] = v;
+    }
+    t.bits = nb;
+    t.eb = eb;
+    t.d = d;
+}
+
+void merge_diagonals(const std::vector<HostGate>& in, std::vector<HostGate>& out) {
+    out.clear();
+    DiagTable open;
+    int n_open = 0;
+    const HostGate* first = nullptr;
+    auto flush = [&]() {
+        if (n_open == 1) {
+            out.push_back(*first);   // a single gate keeps its own form
+        } else if (n_open > 1) {
+            HostGate m;
+            m.kind = 1;
+            m.k = (int)open.eb.size();
+            for (int q = 0; q < m.k; q++) m.ebit[q] = open.eb[(size_t)q];
+            m.mat.resize(2 * open.d.size());
+            for (size_t x = 0; x < open.d.size(); x++) {
+                m.mat[2 * x] = open.d[x].real();
+                m.mat[2 * x + 1] = open.d[x].imag();
+            }
+            out.push_back(std::move(m));
+        }
+        open = DiagTable{};
+        n_open = 0;
+        first = nullptr;
+    };
+    for (const HostGate& h : in) {
+        const bool mergeable = h.kind == 1 && !plain_cz(h) && __builtin_popcountll(gate_bits(h)) <= kMaxMergedDiag;
+        if (mergeable) {
+            if (n_open && __builtin_popcountll(open.bits | gate_bits(h)) > kMaxMergedDiag) flush();
+            if (n_open == 0) first = &h;
+            diag_absorb(open, h);
+            n_open++;
+            continue;
+        }
+        if (n_open && h.kind != 1 && (gate_bits(h) & open.bits)) flush();
+        out.push_back(h);
+    }
+    flush();
+}
+
+}  // namespace
+
 int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     if (sweeps.empty()) return BS_OK;
     const int n_bits = bs_vec_bits(s);
@@ -1193,7 +1289,9 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         for (int b = 0; b < 64; b++) local[b] = -1;
         for (int b = 0; b < L; b++) local[b] = b;
         for (size_t i = 0; i < sw.hi_bits.size(); i++) local[sw.hi_bits[i]] = L + (int)i;
-        const std::vector<HostGate>* glist = (use_tc && fused_ok[si]) ? &fused_all[si] : &sw.gates;
+        std::vector<HostGate> merged;
+        merge_diagonals((use_tc && fused_ok[si]) ? fused_all[si] : sw.gates, merged);
+        const std::vector<HostGate>* glist = &merged;
         for (const HostGate& hg : *glist) {
             if (hg.kind == 5) {
                 // reference-rule channel: its row and column target bits are tile bits (the planner needs them)
