@@ -356,6 +356,14 @@ int bs_apply_kraus(bs_sim* s, const double* kraus, int nk, int k, const int* tar
     return bs_kraus_reference(s, kraus, nk, k, targets, flags);
 }
 
+// A SWAP of two qubits (no controls, no phases) moves no data here: the evolve keeps a map from
+// logical to physical endian bits, relabels every later gate through it, and restores the order
+// once at the end (or before a direct kernel call) with as few physical swaps as the map needs.
+static bool is_plain_swap(const HostGate& g) {
+    return g.kind == 2 && g.k == 2 && g.cmask == 0 && g.perm.size() == 8 && g.perm[0] == 0 && g.perm[1] == 0 &&
+           g.perm[2] == 2 && g.perm[3] == 0 && g.perm[4] == 1 && g.perm[5] == 0 && g.perm[6] == 3 && g.perm[7] == 0;
+}
+
 int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     if (!s) return BS_ERR_INVALID_ARG;
     if (n_ops < 0 || (n_ops > 0 && !ops)) return bs_fail(s, BS_ERR_INVALID_ARG, "bad op list");
@@ -363,7 +371,54 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     if (!s->defer_sync) s->tc_events_used = 0;   // deferred evolves keep their launch events for the caller
     s->alias_valid = false;
     if (!s->capturing) cudaEventRecord(s->ev0, s->stream);
-    std::vector<HostGate> pending;
+    std::vector<HostGate> pending, lowered;
+    const int nb = bs_vec_bits(s);
+    int phys[64];   // physical endian bit of each logical one
+    for (int e = 0; e < 64; e++) phys[e] = e;
+    bool permuted = false;
+    auto relabel = [&](std::vector<HostGate>& gs) {
+        for (HostGate& g : gs) {
+            if (is_plain_swap(g)) {
+                std::swap(phys[g.ebit[0]], phys[g.ebit[1]]);
+                permuted = true;
+                continue;
+            }
+            if (permuted) {
+                const int nbits = g.kind == 5 ? 2 * g.k : g.k;
+                for (int q = 0; q < nbits; q++) g.ebit[q] = phys[g.ebit[q]];
+                uint64_t cm = 0, cv = 0;
+                for (int e = 0; e < 64; e++)
+                    if ((g.cmask >> e) & 1ULL) {
+                        cm |= 1ULL << phys[e];
+                        cv |= ((g.cval >> e) & 1ULL) << phys[e];
+                    }
+                g.cmask = cm;
+                g.cval = cv;
+            }
+            pending.push_back(std::move(g));
+        }
+        gs.clear();
+    };
+    auto restore = [&]() {
+        // physical swaps until logical bit l lives at physical bit l
+        if (!permuted) return;
+        for (int l = 0; l < nb; l++) {
+            if (phys[l] == l) continue;
+            const int p = phys[l];
+            int m = 0;
+            while (phys[m] != l) m++;
+            HostGate g;
+            g.kind = 2;
+            g.k = 2;
+            g.ebit[0] = l;
+            g.ebit[1] = p;
+            g.perm = {0, 0, 2, 0, 1, 0, 3, 0};
+            pending.push_back(std::move(g));
+            phys[l] = l;
+            phys[m] = p;
+        }
+        permuted = false;
+    };
     auto flush = [&]() -> int {
         if (pending.empty()) return BS_OK;
         std::vector<Sweep> sw;
@@ -378,17 +433,18 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
         if (op.kind == 2) continue;
         if (op.kind == 0) {
             rc = bs_lower_gate(s, op.matrix, op.n_targets, op.targets, op.n_controls, op.controls,
-                               op.control_values, op.flags, dm, pending);
+                               op.control_values, op.flags, dm, lowered);
         } else if (op.kind == 1) {
             if (!dm) return bs_fail(s, BS_ERR_STATE, "noise instruction on a state-vector simulator");
             unsigned mode = (op.flags & BS_NOISE_PHYSICAL) ? BS_NOISE_PHYSICAL : noise_mode;
             if (mode & BS_NOISE_PHYSICAL) {
-                rc = bs_lower_kraus_physical(s, op.matrix, op.n_matrices, op.n_targets, op.targets, op.flags, pending);
+                rc = bs_lower_kraus_physical(s, op.matrix, op.n_matrices, op.n_targets, op.targets, op.flags, lowered);
             } else if (s->precision == BS_PREC_C128 && op.n_targets <= 2) {
                 // inside the sweeps (complex128 tile kernels)
                 rc = bs_lower_kraus_reference(s, op.matrix, op.n_matrices, op.n_targets, op.targets, op.flags,
-                                              pending);
+                                              lowered);
             } else {
+                restore();
                 rc = flush();
                 if (!rc) rc = bs_kraus_reference(s, op.matrix, op.n_matrices, op.n_targets, op.targets, op.flags);
             }
@@ -396,7 +452,9 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
             return bs_fail(s, BS_ERR_INVALID_ARG, "unknown op kind");
         }
         if (rc) return rc;
+        relabel(lowered);
     }
+    restore();
     int rc = flush();
     if (rc) return rc;
     if (s->capturing || s->defer_sync) return BS_OK;   // the graph's launcher / the caller synchronises and checks
