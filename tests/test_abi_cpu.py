@@ -111,3 +111,20 @@ def test_multirz_dispatch():
     lg = bs.gates.lower_gate(bs.MultiRZ(0.3, pow_exponent=5.0), [0, 1, 2])
     # pow_exponent is ignored for >= 3 targets, as in the reference
     assert lg[0].diagonal and np.allclose(lg[0].matrix, np.exp(-0.15j * bs.gates.pauli_eigenvalues(3)))
+
+
+def test_new_entry_points_reject_bad_arguments_without_a_gpu_call():
+    """Argument checks of the batch, tuning and partial-trace entry points run on the host and
+    return a status before any device work (NULL handles, bad counts)."""
+    import ctypes as C
+    L = bs._abi.lib()
+    out = C.c_void_p()
+    assert L.bs_batch_create(0, None, None, None, 0, None, None, 0, 0, 0, C.byref(out)) != 0
+    assert L.bs_batch_launch(None, None, None, None) != 0
+    assert L.bs_batch_set_ops(None, None, None) != 0
+    assert L.bs_batch_set_tuning(None, 0, None, None) != 0
+    assert L.bs_batch_destroy(None) == 0
+    v = C.c_double()
+    assert L.bs_set_tuning(None, 0, 1.0) != 0
+    assert L.bs_get_tuning(None, 0, C.byref(v)) != 0
+    assert L.bs_reduced_density_matrix(None, 1, None, None) != 0

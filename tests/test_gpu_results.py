@@ -226,3 +226,11 @@ def test_device_partial_trace_complex64():
     s64.evolve(ops)
     ref = bs.partial_trace(oracle.OracleSV(n).evolve(ops).psi, [2, 7, 11])
     assert np.max(np.abs(s64.reduced_density_matrix([2, 7, 11]) - ref)) < 1e-5
+
+
+def test_device_partial_trace_rejects_bad_qubits():
+    sim = bs.StateVectorSimulator(5, 0)
+    for bad in ([], [5], [1, 1], list(range(13)), [-1]):
+        with pytest.raises(bs._abi.BraketGB300Error):
+            sim.reduced_density_matrix(bad)
+    assert np.allclose(sim.reduced_density_matrix([0]), [[1, 0], [0, 0]])   # the handle stays usable
