@@ -274,6 +274,88 @@ __device__ void tile_kraus_ref(float4* sm, int T, int L, const TileGate& g, cons
 
 // KMAX: widest dense/monomial gate of the sweep (2 or 4); narrow sweeps get a
 // kernel with fewer live registers and therefore more resident warps.
+// The reference-rule Kraus channel of tile_kraus_ref with few registers (for the tensor-core sweep,
+// whose threads have none to spare, and for the float-float sweep, whose 2-target variant would
+// otherwise need the 4-bit kernel): candidate blocks are tested 32 at a time and the ones that pass the
+// row/column test collected, then one thread per output element of a collected block sums over the
+// Kraus matrices reading the block from shared memory; all reads of the collected blocks finish
+// before any of their outputs is written.  s_act: 32 ints of shared scratch.
+template <int K, bool SW, typename OT>
+__device__ void tile_kraus_ref_lr(float4* sm, int T, int L, const TileGate& g, const float4* __restrict__ mats,
+                                  int64_t base, OT off_tab, int osh, int n, int* s_act, int* s_cnt) {
+    constexpr int D = 1 << K, DD = D * D, kChunkG = 32;   // candidate blocks per pass
+    const int64_t rmask = ((int64_t)1 << n) - 1;
+    if ((((base & rmask) ^ (base >> n)) & (int64_t)g.pmask[1]) != 0) return;   // uniform in the CTA
+    int pos[2 * K];
+#pragma unroll
+    for (int q = 0; q < 2 * K; q++) pos[q] = g.tbit[q];
+#pragma unroll
+    for (int a = 0; a < 2 * K; a++)
+#pragma unroll
+        for (int b = a + 1; b < 2 * K; b++)
+            if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
+    const int lowmask = (1 << L) - 1, ngroups = 1 << (T - 2 * K);
+    const float4* km = mats + g.mat_off;
+    for (int gs = 0; gs < ngroups; gs += kChunkG) {   // candidate blocks, one per thread of warp 0
+        if (threadIdx.x == 0) *s_cnt = 0;
+        __syncthreads();
+        if (threadIdx.x < kChunkG) {
+            const int b = gs + (int)threadIdx.x;
+            if (b < ngroups) {
+                int j0 = b;
+#pragma unroll
+                for (int q = 0; q < 2 * K; q++) j0 = insert0(j0, pos[q]);
+                const int64_t gi = base | ((int64_t)off_tab[j0 >> L] << osh) | (int64_t)(j0 & lowmask);
+                if (((((gi & rmask) ^ (gi >> n)) & (int64_t)g.pmask[0]) == 0)) s_act[atomicAdd(s_cnt, 1)] = j0;
+            }
+        }
+        __syncthreads();
+        const int nact = *s_cnt;   // at most kChunkG
+        __syncthreads();           // every thread has read the count before it is reset
+        if (nact > 0) {
+            const int c0 = 0;
+            const int items = nact * DD;
+            for (int it0 = 0; it0 < items; it0 += blockDim.x) {
+                const int it = it0 + (int)threadIdx.x;
+                float4 outv = make_float4(0.f, 0.f, 0.f, 0.f);
+                int dst = -1;
+                if (it < items) {
+                    const int j0 = s_act[c0 + it / DD], e = it % DD, i = e / D, jj = e % D;
+                    auto at = [&](int r, int c) {
+                        int j = j0;
+#pragma unroll
+                        for (int q = 0; q < K; q++) {
+                            if ((r >> q) & 1) j |= 1 << g.tbit[q];
+                            if ((c >> q) & 1) j |= 1 << g.tbit[K + q];
+                        }
+                        return sx<SW>(j);
+                    };
+                    ffacc ar{0.f, 0.f}, ai{0.f, 0.f};
+                    bool first = true;
+                    for (int q = 0; q < g.npar; q++) {
+                        const float4* Kq = km + q * DD;
+                        for (int c = 0; c < D; c++) {
+                            ffacc tr, ti;
+                            cmac_first(tr, ti, f4m(__ldg(Kq + i * D)), f4c(sm[at(0, c)]));
+                            for (int r = 1; r < D; r++) cmac(tr, ti, f4m(__ldg(Kq + i * D + r)), f4c(sm[at(r, c)]));
+                            const cff t = cdone(tr, ti);
+                            const float4 kj = __ldg(Kq + jj * D + c);
+                            const cff kc = {kj.x, kj.y, -kj.z, -kj.w};
+                            if (first) { cmac_first(ar, ai, kc, t); first = false; }
+                            else cmac(ar, ai, kc, t);
+                        }
+                    }
+                    outv = c4f(cdone(ar, ai));
+                    dst = at(i, jj);
+                }
+                __syncthreads();   // every read of this chunk's blocks is done
+                if (dst >= 0) sm[dst] = outv;
+                __syncthreads();
+            }
+        }
+    }
+}
+
 template <int KMAX, int NT>
 __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, SweepDesc d, int64_t tile0) {
     extern __shared__ float4 smem[];
@@ -303,6 +385,7 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
     }
     __syncthreads();
     __shared__ TileGate s_gates[kGateChunk];
+    __shared__ int s_act[32], s_cnt;   // kind 5: blocks passing the row/column test
     for (int g0 = 0; g0 < d.n_gates; g0 += kGateChunk) {
     const int ng = min(kGateChunk, d.n_gates - g0);
     stage_gates(s_gates, d.gates + g0, ng);
@@ -318,8 +401,8 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
         } else if (kind == 1) {
             tile_diag(smem, T, L, g, d.mats, base, off_tab, 0);
         } else if (kind == 5) {
-            if (k == 1) tile_kraus_ref<1, false>(smem, T, L, g, d.mats, base, off_tab, 0, d.n_bits / 2);
-            else if (KMAX > 2) tile_kraus_ref<2, false>(smem, T, L, g, d.mats, base, off_tab, 0, d.n_bits / 2);
+            if (k == 1) tile_kraus_ref_lr<1, false>(smem, T, L, g, d.mats, base, off_tab, 0, d.n_bits / 2, s_act, &s_cnt);
+            else tile_kraus_ref_lr<2, false>(smem, T, L, g, d.mats, base, off_tab, 0, d.n_bits / 2, s_act, &s_cnt);
         } else if (kind == 0) {
             if (k == 1) tile_dense<1>(smem, T, g, d.mats);
             else if (k == 2 || KMAX == 2) tile_dense<2>(smem, T, g, d.mats);
@@ -337,87 +420,6 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
     for (int j = threadIdx.x; j < nt; j += blockDim.x) {
         int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
         __stcs(psi + gidx, store_c128(f4c(smem[j])));
-    }
-}
-
-// The reference-rule Kraus channel of tile_kraus_ref for the tensor-core sweep, whose threads have
-// no registers to spare: candidate blocks are tested 32 at a time and the ones that pass the
-// row/column test collected, then one thread per output element of a collected block sums over the
-// Kraus matrices reading the block from shared memory; all reads of the collected blocks finish
-// before any of their outputs is written.  s_act: 32 ints of shared scratch.
-template <int K, typename OT>
-__device__ void tile_kraus_ref_tc(float4* sm, int T, int L, const TileGate& g, const float4* __restrict__ mats,
-                                  int64_t base, OT off_tab, int n, int* s_act, int* s_cnt) {
-    constexpr int D = 1 << K, DD = D * D, kChunkG = 32;   // candidate blocks per pass
-    const int64_t rmask = ((int64_t)1 << n) - 1;
-    if ((((base & rmask) ^ (base >> n)) & (int64_t)g.pmask[1]) != 0) return;   // uniform in the CTA
-    int pos[2 * K];
-#pragma unroll
-    for (int q = 0; q < 2 * K; q++) pos[q] = g.tbit[q];
-#pragma unroll
-    for (int a = 0; a < 2 * K; a++)
-#pragma unroll
-        for (int b = a + 1; b < 2 * K; b++)
-            if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
-    const int lowmask = (1 << L) - 1, ngroups = 1 << (T - 2 * K);
-    const float4* km = mats + g.mat_off;
-    for (int gs = 0; gs < ngroups; gs += kChunkG) {   // candidate blocks, one per thread of warp 0
-        if (threadIdx.x == 0) *s_cnt = 0;
-        __syncthreads();
-        if (threadIdx.x < kChunkG) {
-            const int b = gs + (int)threadIdx.x;
-            if (b < ngroups) {
-                int j0 = b;
-#pragma unroll
-                for (int q = 0; q < 2 * K; q++) j0 = insert0(j0, pos[q]);
-                const int64_t gi = base | ((int64_t)off_tab[j0 >> L] << L) | (int64_t)(j0 & lowmask);
-                if (((((gi & rmask) ^ (gi >> n)) & (int64_t)g.pmask[0]) == 0)) s_act[atomicAdd(s_cnt, 1)] = j0;
-            }
-        }
-        __syncthreads();
-        const int nact = *s_cnt;   // at most kChunkG
-        __syncthreads();           // every thread has read the count before it is reset
-        if (nact > 0) {
-            const int c0 = 0;
-            const int items = nact * DD;
-            for (int it0 = 0; it0 < items; it0 += blockDim.x) {
-                const int it = it0 + (int)threadIdx.x;
-                float4 outv = make_float4(0.f, 0.f, 0.f, 0.f);
-                int dst = -1;
-                if (it < items) {
-                    const int j0 = s_act[c0 + it / DD], e = it % DD, i = e / D, jj = e % D;
-                    auto at = [&](int r, int c) {
-                        int j = j0;
-#pragma unroll
-                        for (int q = 0; q < K; q++) {
-                            if ((r >> q) & 1) j |= 1 << g.tbit[q];
-                            if ((c >> q) & 1) j |= 1 << g.tbit[K + q];
-                        }
-                        return tc::sw(j);
-                    };
-                    ffacc ar{0.f, 0.f}, ai{0.f, 0.f};
-                    bool first = true;
-                    for (int q = 0; q < g.npar; q++) {
-                        const float4* Kq = km + q * DD;
-                        for (int c = 0; c < D; c++) {
-                            ffacc tr, ti;
-                            cmac_first(tr, ti, f4m(__ldg(Kq + i * D)), f4c(sm[at(0, c)]));
-                            for (int r = 1; r < D; r++) cmac(tr, ti, f4m(__ldg(Kq + i * D + r)), f4c(sm[at(r, c)]));
-                            const cff t = cdone(tr, ti);
-                            const float4 kj = __ldg(Kq + jj * D + c);
-                            const cff kc = {kj.x, kj.y, -kj.z, -kj.w};
-                            if (first) { cmac_first(ar, ai, kc, t); first = false; }
-                            else cmac(ar, ai, kc, t);
-                        }
-                    }
-                    outv = c4f(cdone(ar, ai));
-                    dst = at(i, jj);
-                }
-                __syncthreads();   // every read of this chunk's blocks is done
-                if (dst >= 0) sm[dst] = outv;
-                __syncthreads();
-            }
-        }
     }
 }
 
@@ -538,8 +540,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
         } else if (kind == 1) {
             tile_diag<HiOff, true>(smem, T, L, g, d.mats, base, off32, L);
         } else if (kind == 5) {
-            if (k == 1) tile_kraus_ref_tc<1, HiOff>(smem, T, L, g, d.mats, base, off32, d.n_bits / 2, s_act, &s_cnt);
-            else tile_kraus_ref_tc<2, HiOff>(smem, T, L, g, d.mats, base, off32, d.n_bits / 2, s_act, &s_cnt);
+            if (k == 1) tile_kraus_ref_lr<1, true, HiOff>(smem, T, L, g, d.mats, base, off32, L, d.n_bits / 2, s_act, &s_cnt);
+            else tile_kraus_ref_lr<2, true, HiOff>(smem, T, L, g, d.mats, base, off32, L, d.n_bits / 2, s_act, &s_cnt);
 
         } else if (kind == 0) {   // the planner routes sweeps with unfused 3- or 4-target gates elsewhere
             if (k == 1) tile_dense<1, true>(smem, T, g, d.mats);
@@ -1311,7 +1313,6 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
                 t.npar = (int32_t)(hg.mat.size() / (size_t)(2 * D * D));
                 t.mat_off = (int32_t)mats.size();
                 for (size_t e = 0; e + 1 < hg.mat.size(); e += 2) mats.push_back(to_cff(hg.mat[e], hg.mat[e + 1]));
-                ln.kmax = std::max(ln.kmax, 2 * hg.k);
                 tg.push_back(t);
                 ln.n_gates++;
                 continue;
