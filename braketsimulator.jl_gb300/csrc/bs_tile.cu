@@ -1187,6 +1187,20 @@ void merge_diagonals(const std::vector<HostGate>& in, std::vector<HostGate>& out
     DiagTable open;
     int n_open = 0;
     const HostGate* first = nullptr;
+    // CZ gates float forward the same way and are emitted together sorted by the distance of their
+    // two bits, so that the packer folds each distance into one parity-phase term
+    std::vector<const HostGate*> czs;
+    uint64_t cz_bits = 0;
+    auto cz_dist = [](const HostGate* h) {
+        const int c = 63 - __builtin_clzll(h->cmask), t = h->ebit[0];
+        return c > t ? c - t : t - c;
+    };
+    auto flush_cz = [&]() {
+        std::stable_sort(czs.begin(), czs.end(), [&](const HostGate* a, const HostGate* b) { return cz_dist(a) < cz_dist(b); });
+        for (const HostGate* h : czs) out.push_back(*h);
+        czs.clear();
+        cz_bits = 0;
+    };
     auto flush = [&]() {
         if (n_open == 1) {
             out.push_back(*first);   // a single gate keeps its own form
@@ -1207,7 +1221,12 @@ void merge_diagonals(const std::vector<HostGate>& in, std::vector<HostGate>& out
         first = nullptr;
     };
     for (const HostGate& h : in) {
-        const bool mergeable = h.kind == 1 && !plain_cz(h) && __builtin_popcountll(gate_bits(h)) <= kMaxMergedDiag;
+        if (plain_cz(h)) {
+            czs.push_back(&h);
+            cz_bits |= gate_bits(h);
+            continue;
+        }
+        const bool mergeable = h.kind == 1 && __builtin_popcountll(gate_bits(h)) <= kMaxMergedDiag;
         if (mergeable) {
             if (n_open && __builtin_popcountll(open.bits | gate_bits(h)) > kMaxMergedDiag) flush();
             if (n_open == 0) first = &h;
@@ -1215,10 +1234,14 @@ void merge_diagonals(const std::vector<HostGate>& in, std::vector<HostGate>& out
             n_open++;
             continue;
         }
-        if (n_open && h.kind != 1 && (gate_bits(h) & open.bits)) flush();
+        if (h.kind != 1) {
+            if (n_open && (gate_bits(h) & open.bits)) flush();
+            if (!czs.empty() && (gate_bits(h) & cz_bits)) flush_cz();
+        }
         out.push_back(h);
     }
     flush();
+    flush_cz();
 }
 
 }  // namespace
