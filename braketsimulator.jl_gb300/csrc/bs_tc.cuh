@@ -15,14 +15,16 @@
 // power of two and every partial sum below 2^24 of it, so these FP32 sums are
 // exact) and i+j = 4, 5, 6 together (rounding at 2^-56 of the result).  After
 // each round the CUDA cores fold the FP32 accumulator into a running
-// float-float sum, while the tensor cores run the next round into the other
-// of two accumulators.  What remains is the 48-bit truncation of both operands,
-// ~2^-46 of the tile's largest value per fused gate.
+// float-float sum, while the tensor cores run other rounds in the other of two
+// accumulators; two threads issue, one per accumulator, so that neither chain
+// of issue, fold and re-issue waits for the other.  What remains is the 48-bit
+// truncation of both operands, ~2^-46 of the tile's largest value per fused gate.
 //
 // TMEM (256 columns per CTA, so that two CTAs share an SM and one's MMAs
 // overlap the other's CUDA-core work):
 //   D0, D1 (FP32 accumulators, lane m): columns 0..63, and columns 192..255 once
-//     round 4, the only reader of A digit slices 4 and 5, has completed.
+//     the MMAs of round 4 that read A digit slices 4 and 5 (the only readers of
+//     those slices, issued first) have completed.
 //   A (state digits): lanes 0..127 = columns m, TMEM columns kA0 + 32 j + t hold
 //     (Re, Im) of digit j of amplitude t as a bf16 pair (low half = Re).
 // B (matrix digits): shared memory, K-major, no swizzle: 8x8 core matrices of
@@ -209,75 +211,124 @@ __device__ __forceinline__ f2 two_sum2(f2& s, f2 g) {
 
 struct State {
     uint32_t tmem;   // TMEM base address
-    uint32_t bar;    // five mbarriers 8 bytes apart: digit-slice copy (1 arrival + bytes), MMAs done into
-                     // D0, into D1 (commits), D0 read, D1 read (one arrival per warp)
+    uint32_t bar;    // seven mbarriers 8 bytes apart: digit-slice copy (1 arrival + bytes), MMAs done into
+                     // D0, into D1 (commits), D0 read, D1 read (one arrival per warp), round 4's
+                     // state-digit-4/5 MMAs done, round 0 done into D2 (commits)
     uint32_t ph;     // expected phase parity of barrier k in bit k
+    bool pref;       // the digit slices of the gate about to run were copied ahead (uniform)
 };
 
 constexpr uint32_t kD1 = kA0 + 128;   // second accumulator: the columns of A digit slices 4 and 5
+constexpr uint32_t kD2 = kA0 + 64;    // third accumulator (round 0 only): the columns of A digit slices 2 and 3
 
-// Thread 0: issue the MMAs of one digit-weight round into the accumulator at TMEM column dcol,
-// then commit to bar.  The round is a compile-time constant so that the loops unroll and every
-// operand address is the base plus a constant: a single thread issues back to back (a run-time
-// loop here doubled the time per MMA).  b0 = descriptor of the first digit slice; slice (i, s)
-// starts (i*4+s)*2048 bytes later, which adds (i*4+s)*128 to the 14-bit start-address field
+// Source of a fused gate's digit slices for the CTA: the matrix variant selected by the base bits.
+__device__ __forceinline__ const uint16_t* slice_src(const TileGate& g, const uint16_t* pool, int64_t base) {
+    const int nu = g.tc_nu;
+    int var = 0;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+        if (i < nu) var |= (int)((base >> g.tc_ub[i]) & 1) << i;
+    return pool + (size_t)(g.tc_off + var) * kPoolBlock;
+}
+// One thread: the 48 KiB of digit slices into sB, completing on barrier bar.
+__device__ __forceinline__ void copy_slices(uint32_t sB, const uint16_t* src, uint32_t bar) {
+    mbar_expect_tx(bar, (uint32_t)kPoolBlock * 2);
+    bulk_g2s(sB, src, (uint32_t)kPoolBlock * 2, bar);
+}
+
+// One thread issues the MMAs of the digit pairs (i, j) with G0 <= i + j <= G1 and JLO <= j <= JHI
+// (j: state digit, i: matrix digit) into the accumulator at TMEM column dcol; the first one
+// overwrites when OVERWRITE.  The pair set is a compile-time constant so that the loops unroll and
+// every operand address is the base plus a constant: a single thread issues back to back (a
+// run-time loop here doubled the time per MMA).  b0 = descriptor of the first digit slice; slice
+// (i, s) starts (i*4+s)*2048 bytes later, which adds (i*4+s)*128 to the 14-bit start-address field
 // without carry (the slices span 48 KiB).
-template <int ROUND>
-__device__ __forceinline__ void issue_round(uint32_t tmem, uint32_t dcol, uint64_t b0_, uint32_t bar) {
-    constexpr int g0 = ROUND < 4 ? ROUND : 4, g1 = ROUND < 4 ? ROUND : 6;
+template <int G0, int G1, int JLO, int JHI, bool OVERWRITE>
+__device__ __forceinline__ void issue_pairs(uint32_t tmem, uint32_t dcol, uint64_t b0_) {
     // an opaque copy, so that the descriptors are formed here and not hoisted into registers
-    // held across the caller's loop
+    // held across the caller's code
     uint64_t b0;
     asm volatile("mov.b64 %0, %1;" : "=l"(b0) : "l"(b0_));
     int n = 0;
 #pragma unroll
-    for (int gs = g0; gs <= g1; gs++)
+    for (int gs = G0; gs <= G1; gs++)
 #pragma unroll
         for (int j = 0; j <= gs; j++)
 #pragma unroll
             for (int s = 0; s < 4; s++) {
                 const int i = gs - j;
-                if (i > 5 || j > 5) continue;
+                if (i > 5 || j > 5 || j < JLO || j > JHI) continue;
                 mma(tmem + dcol, tmem + (uint32_t)(kA0 + 32 * j + 8 * s), b0 + (uint64_t)((i * 4 + s) * 128),
-                    n == 0 ? 0u : 1u);
+                    (OVERWRITE && n == 0) ? 0u : 1u);
                 n++;
             }
+}
+// Round r < 4: the pairs of weight r, overwriting the accumulator, then a commit to bar.
+template <int ROUND>
+__device__ __forceinline__ void issue_round(uint32_t tmem, uint32_t dcol, uint64_t b0, uint32_t bar) {
+    issue_pairs<ROUND, ROUND, 0, 5, true>(tmem, dcol, b0);
     commit(bar);
 }
-__device__ __forceinline__ void issue(uint32_t tmem, uint32_t dcol, uint64_t b0, uint32_t bar, int round) {
-    switch (round) {
-        case 0: issue_round<0>(tmem, dcol, b0, bar); break;
-        case 1: issue_round<1>(tmem, dcol, b0, bar); break;
-        case 2: issue_round<2>(tmem, dcol, b0, bar); break;
-        case 3: issue_round<3>(tmem, dcol, b0, bar); break;
-        default: issue_round<4>(tmem, dcol, b0, bar); break;
+
+// Fold of one round's accumulator columns (this thread's NA amplitudes, re and im packed) into the
+// float-float sums: MODE 0: E = D, 1: E += D, 2: S = D, 3: E += TwoSum(S, D) error with S updated.
+template <int MODE, int NA>
+__device__ __forceinline__ void fold(uint32_t taddr, f2 (&S)[NA], f2 (&E)[NA]) {
+#pragma unroll
+    for (int c2 = 0; c2 < NA / 4; c2 += 2) {   // two 8-column loads in flight, one wait
+        uint32_t r[2][8];
+        ld8(taddr + (uint32_t)(8 * c2), r[0]);
+        ld8(taddr + (uint32_t)(8 * c2 + 8), r[1]);
+        wait_ld16(r[0], r[1]);
+#pragma unroll
+        for (int u = 0; u < 2; u++)
+#pragma unroll
+            for (int p = 0; p < 4; p++) {
+                const int o = 4 * (c2 + u) + p;
+                const f2 gv = pk(__uint_as_float(r[u][2 * p]), __uint_as_float(r[u][2 * p + 1]));
+                if (MODE == 0) E[o] = gv;
+                else if (MODE == 1) E[o] = add2(E[o], gv);
+                else if (MODE == 2) S[o] = gv;
+                else E[o] = add2(E[o], two_sum2(S[o], gv));
+            }
     }
+}
+
+// Warp-uniform bounded wait on barrier k of the state for its expected parity, then the parity flips.
+__device__ __forceinline__ bool wait_bar(State& st, int k, int lane_id) {
+    uint32_t done = 1;
+    if (lane_id == 0) done = mbar_wait(st.bar + 8u * (uint32_t)k, (st.ph >> k) & 1u) ? 1u : 0u;
+    done = __shfl_sync(0xffffffffu, done, 0);
+    st.ph ^= 1u << k;
+    fence_after();
+    return done != 0;
+}
+// One thread's bounded wait (the parity flip is left to the caller, which flips it on every thread).
+__device__ __forceinline__ bool wait_bar1(const State& st, int k) {
+    const bool ok = mbar_wait(st.bar + 8u * (uint32_t)k, (st.ph >> k) & 1u);
+    fence_after();
+    return ok;
 }
 
 // Applies fused gate g to the (swizzled) 2^12 tile sm of float4 (re hi, im hi, re lo, im lo).
 // Called by all NT threads of the CTA (NT/128 threads per tile column, 32*128/NT amplitudes each),
 // which then synchronise.  base: the CTA's global base index (selects the matrix variant).  s_tsw:
 // 32 ints of shared scratch; s_wmax: NT/32 per-warp maxima of the high words' exponent fields.
+// gnext: the tile's next fused gate, whose digit slices are copied ahead as soon as this gate's
+// MMAs have completed (null: none, or it copies its own); s_nsrc: shared scratch for their source.
 // The swizzle is linear over XOR, so the position of column m's amplitude t is
 // sw(column bits) ^ sw(target bits of t).
 // On a wait that gives up, sets *fail and *err and leaves the tile partly updated.
 template <int NT>
-__device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint16_t* __restrict__ pool, uint16_t* sB,
-                                      State& st, int64_t base, uint32_t* s_wmax, bool emax_ok, int* s_tsw,
-                                      int* s_fail, int* err) {
+__device__ __forceinline__ void apply(float4* sm, const TileGate& g, const TileGate* gnext,
+                                      const uint16_t* __restrict__ pool, uint16_t* sB, State& st, int64_t base,
+                                      uint32_t* s_wmax, bool emax_ok, int* s_tsw, const uint16_t** s_nsrc, int* s_fail,
+                                      int* err) {
     constexpr int HP = NT / 128;   // threads per column
     constexpr int NA = 32 / HP;    // amplitudes per thread
     const int tid = threadIdx.x, warp = tid >> 5, lane_id = tid & 31, m = tid & 127, h = tid >> 7;
-    if (tid < 6) {
-        // the previous readers of sB (the MMAs of the previous fused gate) have completed; lanes 0..5
-        // each copy one 8 KiB digit slice of the CTA's matrix variant
-        int var = 0;
-        for (int i = 0; i < g.tc_nu; i++) var |= (int)((base >> g.tc_ub[i]) & 1) << i;
-        if (tid == 0) mbar_expect_tx(st.bar, (uint32_t)kPoolBlock * 2);
-        __syncwarp(0x3fu);
-        const uint16_t* src = pool + (size_t)(g.tc_off + var) * kPoolBlock;
-        bulk_g2s(su32(sB) + (uint32_t)tid * 8192u, src + tid * 4096, 8192u, st.bar);
-    }
+    // the previous readers of sB (the MMAs of the previous fused gate) have completed
+    if (!st.pref && tid == 0) copy_slices(su32(sB), slice_src(g, pool, base), st.bar);
     int tb[5];
     uint32_t tmask = 0;
 #pragma unroll
@@ -342,66 +393,75 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const uint1
     __syncthreads();
     fence_after();
     const uint64_t b0 = bdesc(su32(sB));
-    if (tid == 0) {
-        if (mbar_wait(st.bar, st.ph & 1u)) issue_round<4>(st.tmem, 0u, b0, st.bar + 8u);
-        else { *s_fail = 1; atomicExch(err, 1); }
-    }
-    st.ph ^= 1u;
-    __syncthreads();
-    if (*s_fail) return;
-    // The rounds run in the order 4, 3, 2, 1, 0 (smallest digit weights first) into two
-    // accumulators: D0 (columns 0..63) takes rounds 4, 2 and 0; D1 takes rounds 3 and 1, in the
-    // columns of A digit slices 4 and 5, which only round 4 reads.  Round 3 is issued as soon as
-    // round 4 has completed; every later round as soon as all warps have read the accumulator it
-    // reuses, so that the MMAs of one round run while the warps fold the previous one into their
-    // float-float sums (the thread's amplitudes, re and im packed).
-    f2 S[NA], E[NA];
+    // Round 4 (weights 4..6, 64 MMAs) into D0 by thread 0: first the 20 MMAs that read state digits 4
+    // and 5, committed to barrier 5, so that D1, which takes their columns, is free once they have
+    // completed; thread 128 then issues round 3 into D1 while thread 0 still issues round 4.  Two
+    // issuers, each waiting only for the reads of its own accumulator: thread 0 runs D0 (rounds 4,
+    // 1), thread 128 runs D1 (rounds 3, 2) and round 0 into D2, the columns of state digits 2 and 3,
+    // which are free once rounds 4, 3 and 2 have completed.  Every warp folds the rounds in the order
+    // 4, 3, 2, 1, 0 (smallest digit weights first), E collecting rounds 4 and 3 in FP32 and S rounds
+    // 2, 1, 0 with their TwoSum errors into E.
     bool ok = true;
-#pragma unroll
-    for (int k = 0; k < 5; k++) {   // unrolled: each step's fold and issue are then fixed code (a run-time k spilled)
-        const int acc = k & 1;
-        const uint32_t dcol = acc ? kD1 : 0u;
-        const uint32_t bm = st.bar + 8u * (1 + acc), br = st.bar + 8u * (3 + acc);
-        const uint32_t mbit = 2u << acc, rbit = 8u << acc;
-        uint32_t done = 1;
-        if (lane_id == 0) done = mbar_wait(bm, (st.ph & mbit) ? 1u : 0u) ? 1u : 0u;
-        done = __shfl_sync(0xffffffffu, done, 0);
-        st.ph ^= mbit;
-        if (!done) { ok = false; break; }
-        fence_after();
-        if (k == 0 && tid == 0) issue_round<3>(st.tmem, kD1, b0, st.bar + 16u);
-#pragma unroll
-        for (int c2 = 0; c2 < NA / 4; c2 += 2) {   // two 8-column loads in flight, one wait
-            uint32_t r[2][8];
-            ld8(st.tmem + lane + dcol + (uint32_t)(2 * NA * h + 8 * c2), r[0]);
-            ld8(st.tmem + lane + dcol + (uint32_t)(2 * NA * h + 8 * c2 + 8), r[1]);
-            wait_ld16(r[0], r[1]);
-#pragma unroll
-            for (int u = 0; u < 2; u++)
-#pragma unroll
-                for (int p = 0; p < 4; p++) {
-                    const int o = 4 * (c2 + u) + p;
-                    const f2 gv = pk(__uint_as_float(r[u][2 * p]), __uint_as_float(r[u][2 * p + 1]));
-                    if (k == 0) E[o] = gv;
-                    else if (k == 1) E[o] = add2(E[o], gv);
-                    else if (k == 2) S[o] = gv;
-                    else E[o] = add2(E[o], two_sum2(S[o], gv));
-                }
+    if (tid == 0) {
+        if (mbar_wait(st.bar, st.ph & 1u)) {
+            fence_after();
+            issue_pairs<4, 6, 4, 5, true>(st.tmem, 0u, b0);
+            commit(st.bar + 40u);
+            issue_pairs<4, 6, 0, 3, false>(st.tmem, 0u, b0);
+            commit(st.bar + 8u);
+        } else {
+            ok = false;
         }
+    } else if (tid == 128) {
+        if (wait_bar1(st, 5)) issue_round<3>(st.tmem, kD1, b0, st.bar + 16u);
+        else ok = false;
+        if (gnext) *s_nsrc = slice_src(*gnext, pool, base);   // read back by this thread only
+    }
+    st.ph ^= 1u | (1u << 5);
+    if (!ok) { *s_fail = 1; atomicExch(err, 1); }
+    f2 S[NA], E[NA];
+    const uint32_t tl = st.tmem + lane + (uint32_t)(2 * NA * h);
+    // round 4 (D0)
+    ok = wait_bar(st, 1, lane_id);
+    if (ok) {
+        fold<0>(tl, S, E);
         fence_before();
         __syncwarp();
-        if (lane_id == 0) mbar_arrive(br);
-        if (k + 2 <= 4 && tid == 0) {
-            if (mbar_wait(br, (st.ph & rbit) ? 1u : 0u)) {
-                fence_after();
-                issue(st.tmem, dcol, b0, bm, 2 - k);
-            } else {
-                ok = false;
-            }
-        }
-        st.ph ^= rbit;
-        if (!ok) break;
+        if (lane_id == 0) mbar_arrive(st.bar + 24u);
     }
+    // round 3 (D1)
+    if (ok) ok = wait_bar(st, 2, lane_id);
+    if (ok) {
+        fold<1>(tl + kD1, S, E);
+        fence_before();
+        __syncwarp();
+        if (lane_id == 0) mbar_arrive(st.bar + 32u);
+        // each issuer has already arrived for its own warp
+        if (tid == 0) {
+            if (wait_bar1(st, 3)) issue_round<1>(st.tmem, 0u, b0, st.bar + 8u);
+            else ok = false;
+        } else if (tid == 128) {
+            if (wait_bar1(st, 4)) issue_round<2>(st.tmem, kD1, b0, st.bar + 16u);
+            else ok = false;
+        }
+    }
+    st.ph ^= (1u << 3) | (1u << 4);
+    // round 2 (D1); once it has completed, round 0 goes into D2
+    if (ok) ok = wait_bar(st, 2, lane_id);
+    if (ok) {
+        if (tid == 128) issue_round<0>(st.tmem, kD2, b0, st.bar + 48u);
+        fold<2>(tl + kD1, S, E);
+    }
+    // round 1 (D0), round 0 (D2)
+    if (ok) ok = wait_bar(st, 1, lane_id);
+    if (ok) fold<3>(tl, S, E);
+    if (ok) ok = wait_bar(st, 6, lane_id);
+    if (ok) {
+        // every MMA of this gate has completed: sB takes the next gate's digit slices
+        if (tid == 128 && gnext) copy_slices(su32(sB), *s_nsrc, st.bar);
+        fold<3>(tl + kD2, S, E);
+    }
+    st.pref = ok && gnext != nullptr;
     if (!ok) {
         *s_fail = 1;
         atomicExch(err, 1);

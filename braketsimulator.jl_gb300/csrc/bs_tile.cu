@@ -448,7 +448,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
     extern __shared__ __align__(128) unsigned char dsm[];
     uint16_t* sB = reinterpret_cast<uint16_t*>(dsm);
     float4* smem = reinterpret_cast<float4*>(dsm + 49152);
-    __shared__ __align__(8) uint64_t bars[5];   // digit copy, MMAs into D0 / D1, D0 / D1 read
+    __shared__ __align__(8) uint64_t bars[7];   // digit copy, MMAs into D0 / D1, D0 / D1 read, D1 free, D2
     __shared__ uint32_t s_tmem;
     __shared__ int64_t s_base;
     __shared__ int s_fail;
@@ -456,6 +456,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
     __shared__ uint32_t s_offa[8], s_offb[16];
     __shared__ uint32_t s_wmax[kTcThreads / 32];   // per-warp largest high-word exponent field
     __shared__ int s_act[32], s_cnt;                 // kind 5: blocks passing the row/column test
+    __shared__ int s_tcq[16], s_ntc;                 // the tile's first 16 fused gates, in order
+    __shared__ const uint16_t* s_nsrc;
     const HiOff off32{s_offa, s_offb};
     constexpr int T = 12, L = 5, H = 7, nt = 1 << T, lowmask = (1 << L) - 1;
     const int64_t tile = tile0 + (int64_t)blockIdx.x;
@@ -471,6 +473,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
         tc::mbar_init(tc::su32(&bars[2]));
         tc::mbar_init_n(tc::su32(&bars[3]), kTcThreads / 32);
         tc::mbar_init_n(tc::su32(&bars[4]), kTcThreads / 32);
+        tc::mbar_init(tc::su32(&bars[5]));
+        tc::mbar_init(tc::su32(&bars[6]));
     }
     if (threadIdx.x < 24) {
         const int i = threadIdx.x < 8 ? threadIdx.x : (threadIdx.x - 8) << 3;
@@ -492,6 +496,31 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
             const int j = i * kTcThreads + (int)threadIdx.x;
             x[i] = __ldcs(psi + (base | ((int64_t)off32[j >> L] << L) | (int64_t)(j & lowmask)));
         }
+        if (warp == kTcThreads / 32 - 1) {
+            // while the loads are in flight: the fused gates this tile runs (those whose controls its
+            // base satisfies), and the copy of the first one's digit slices
+            const int lane = threadIdx.x & 31;
+            int cnt = 0, first = -1;
+            for (int c0 = 0; c0 < d.n_gates; c0 += 32) {
+                const int gi = c0 + lane;
+                bool f = false;
+                if (gi < d.n_gates) {
+                    const TileGate& g = d.gates[gi];
+                    f = g.kind == 4 && (base & (int64_t)g.gc_mask) == (int64_t)g.gc_val;
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, f);
+                if (f) {
+                    const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+                    if (pos < 16) s_tcq[pos] = gi;
+                }
+                if (first < 0 && bal) first = c0 + __ffs((int)bal) - 1;
+                cnt += __popc(bal);
+            }
+            if (lane == 0) {
+                s_ntc = cnt < 16 ? cnt : 16;
+                if (first >= 0) tc::copy_slices(tc::su32(sB), tc::slice_src(d.gates[first], d.tc_pool, base), tc::su32(&bars[0]));
+            }
+        }
         uint32_t eb = 0;
 #pragma unroll
         for (int i = 0; i < NL; i++) {
@@ -503,7 +532,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
         if ((threadIdx.x & 31) == 0) s_wmax[threadIdx.x >> 5] = eb;
     }
     __syncthreads();
-    tc::State st{0u, tc::su32(&bars[0]), 0u};
+    tc::State st{0u, tc::su32(&bars[0]), 0u, s_ntc > 0};
+    int q = 0;   // fused gates run so far
     bool have = false;
     bool emax_ok = true;   // s_wmax holds the tile's largest exponent (no magnitude-changing gate since)
     for (int gi = 0; gi < d.n_gates; gi++) {
@@ -521,7 +551,10 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
                 st.tmem = s_tmem;
                 have = true;
             }
-            tc::apply<kTcThreads>(smem, g, d.tc_pool, sB, st, base, s_wmax, emax_ok, s_tsw, &s_fail, d.err);
+            const TileGate* gn = q + 1 < s_ntc ? d.gates + s_tcq[q + 1] : nullptr;
+            tc::apply<kTcThreads>(smem, g, gn, d.tc_pool, sB, st, base, s_wmax, emax_ok, s_tsw, &s_nsrc, &s_fail,
+                                  d.err);
+            q++;
             emax_ok = true;
             if (gi == tc_last) {
                 __syncthreads();
@@ -558,6 +591,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
             tc::mbar_wait(st.bar, st.ph & 1u);
             tc::mbar_wait(st.bar + 8u, (st.ph >> 1) & 1u);
             tc::mbar_wait(st.bar + 16u, (st.ph >> 2) & 1u);
+            tc::mbar_wait(st.bar + 48u, (st.ph >> 6) & 1u);
         }
         __syncthreads();
         if (warp == 0) tc::tmem_dealloc(st.tmem);
