@@ -130,9 +130,18 @@ def peaks():
 
 # Tensor-core sweep (k_tile_sweep_tc): executed bf16 MMA work per fused gate per 2^12-amplitude tile
 # (26 digit pairs x 4 k-steps, each M=128 N=64 K=16), and the DRAM bytes per amplitude per launch that
-# ncu measured for it on the 26-qubit dense circuit (1.0747e9 read + 1.0120e9 written per launch).
+# ncu measured for it on the 27-qubit dense circuit (2.1488e9 read + 2.0865e9 written per launch).
 TC_FLOP_PER_TILE_GATE = 104 * 2 * 128 * 64 * 16
-TC_DRAM_BYTES_PER_AMP = (1.074702e9 + 1.012025e9) / 2 ** 26
+TC_DRAM_BYTES_PER_AMP = (2.148804e9 + 2.086545e9) / 2 ** 27
+
+
+def workload_name():
+    return f"dense random circuit, {N_QUBITS} qubits, complex128, 2x20 layers, <Z0 Z{N_QUBITS - 1}> + 1e5 shots"
+
+
+def l2_note():
+    gib = 16 * 2 ** N_QUBITS / 2 ** 30
+    return f"state ({gib:g} GiB) larger than L2 (129 MB)"
 
 
 def step(bs, sim, ops, shots, seed):
@@ -386,7 +395,7 @@ def run_reference(args, rank, world):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1000 * float(np.mean([dt for _, dt in vals])), 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64)", "data": "synthetic",
-            "config": {"workload": "dense random circuit, 30 qubits, complex128, 2x20 layers, <Z0 Z29> + 1e5 shots",
+            "config": {"workload": workload_name(),
                        "qubits": N_QUBITS, "shots": SHOTS,
                        "bytes": "gate-layer bytes: 2*16*2^n per gate (one pass per gate, as the reference runs)",
                        "sample": "each step times a bounded run of the workload's gate sweeps (SU(2) and CZ "
@@ -486,10 +495,10 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * wall / args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c128 state, float-float (FP32-pipe) arithmetic", "data": "synthetic (seeded Haar SU(2) + CZ)",
-        "config": {"workload": "dense random circuit, 30 qubits, complex128, 2x20 layers, <Z0 Z29> + 1e5 shots",
+        "config": {"workload": workload_name(),
                    "qubits": N_QUBITS, "gates": n_gates, "shots": SHOTS,
                    "bytes": "gate-layer bytes: 2*16*2^n per gate (one pass per gate, as the reference runs)",
-                   "l2": "state (16 GiB) larger than L2 (129 MB)", "parallelism": "replicas" if world > 1 else "1 GPU"},
+                   "l2": l2_note(), "parallelism": "replicas" if world > 1 else "1 GPU"},
         "e2e": {"value": round(e2e, 1), "unit": "GB/s", "h2d_bytes_per_step": int(n_gates * 64 + 200 * n_gates),
                 "d2h_bytes_per_step": int(SHOTS * 8 + 8)},
         "roofline": roofline,

@@ -17,7 +17,8 @@ from .simulators import (DensityMatrixSimulator, Instruction, StateVectorSimulat
 from .results import (Amplitude, DensityMatrix, Expectation, Probability, Sample, StateVector, Variance,  # noqa: F401
                       calculate, marginal_probability, partial_trace, permute_density_matrix, permute_probability)
 from .adjoint import adjoint_gradient, energy_rrule, parameter_shift_gradient, torch_energy  # noqa: F401
-from .program import Program, simulate, create_sim  # noqa: F401
+from .program import (Circuit, Program, basis_rotation_gates, create_sim, fix_endianness, simulate,  # noqa: F401
+                      tensor_product_index_dict)
 from .batch import CapturedBatch, batch_simulate  # noqa: F401
 from .autotune import autotune, get_tuning, set_tuning  # noqa: F401
 

@@ -10,7 +10,9 @@
 // bits share the read.  Every kernel is templated on the storage (complex128 or
 // complex64); sums are carried in float-float, i.e. at FP64-level accuracy.
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <map>
 #include <vector>
 #include "bs_internal.h"
@@ -41,6 +43,19 @@ template <bool C64>
 __global__ void k_prob_dm(const typename Elem<C64>::T* __restrict__ S, double* __restrict__ out, int64_t dim) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = (double)S[i * (dim + 1)].x;
+}
+
+// One chunk [i0, i0 + cnt) of a result written to a file: mode 0 the state vector as complex128,
+// 1 its probabilities, 2 the probabilities (diagonal) of a density matrix of side dim.
+template <bool C64>
+__global__ void k_file_chunk(const typename Elem<C64>::T* __restrict__ st, int mode, int64_t dim, int64_t i0,
+                             int64_t cnt, void* __restrict__ out) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < cnt; j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = i0 + j;
+        if (mode == 0) reinterpret_cast<double2*>(out)[j] = make_double2((double)st[i].x, (double)st[i].y);
+        else if (mode == 1) reinterpret_cast<double*>(out)[j] = prob_of<C64>(st[i]);
+        else reinterpret_cast<double*>(out)[j] = (double)st[i * (dim + 1)].x;
+    }
 }
 
 struct TermSet {
@@ -394,6 +409,71 @@ int bs_marginal_probabilities(bs_sim* s, int k, const int* targets, double* host
     rc = bs_cuda_check(s, cudaMemcpyAsync(host_out, partial + (int64_t)nb * D, (size_t)D * 8, cudaMemcpyDeviceToHost, s->stream), "marginal");
     if (rc) return rc;
     return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "marginal sync");
+}
+
+// Large results straight from the device to a file (the reference writes result values above
+// 1 MiB to temporary files for its external callers, _mmap_large_result_values,
+// src/BraketSimulator.jl:410-428).  Chunks go through two pinned buffers, so that the copy of one
+// overlaps the write of the other; no host copy of the whole result is made.
+int bs_write_result_file(bs_sim* s, int what, const char* path, int64_t* bytes_out) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (!path) return bs_fail(s, BS_ERR_INVALID_ARG, "null path");
+    if (what != BS_FILE_STATE && what != BS_FILE_PROBABILITIES) return bs_fail(s, BS_ERR_INVALID_ARG, "unknown result kind");
+    if (what == BS_FILE_STATE && s->kind != BS_KIND_SV)
+        return bs_fail(s, BS_ERR_INVALID_ARG, "the state-vector file needs a state-vector simulator");
+    const bool c64 = s->precision == BS_PREC_C64, dm = s->kind == BS_KIND_DM;
+    const int64_t dim = (int64_t)1 << s->n;
+    const int64_t eb = what == BS_FILE_STATE ? 16 : 8, ch = ((int64_t)32 << 20) / eb;
+    const bool direct = what == BS_FILE_STATE && !c64;   // complex128 state: plain copies
+    if (!direct) {
+        const int rc = bs_ensure_scratch(s, 2 * ch * eb);
+        if (rc) return rc;
+    }
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return bs_fail(s, BS_ERR_IO, std::string("cannot open ") + path);
+    void* hb[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    int rc = BS_OK;
+    int64_t pending = -1;   // chunk whose copy is in flight in slot pending & 1
+    for (int i = 0; i < 2 && !rc; i++) {
+        rc = bs_cuda_check(s, cudaHostAlloc(&hb[i], (size_t)(ch * eb), cudaHostAllocDefault), "file staging");
+        if (!rc) rc = bs_cuda_check(s, cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming), "file staging");
+    }
+    auto flush = [&](int64_t k) {
+        const int slot = (int)(k & 1);
+        const int64_t cnt = std::min<int64_t>(ch, dim - k * ch);
+        int r = bs_cuda_check(s, cudaEventSynchronize(ev[slot]), "file copy");
+        if (!r && std::fwrite(hb[slot], (size_t)eb, (size_t)cnt, f) != (size_t)cnt) r = bs_fail(s, BS_ERR_IO, std::string("write failed: ") + path);
+        return r;
+    };
+    const int mode = what == BS_FILE_STATE ? 0 : (dm ? 2 : 1);
+    for (int64_t k = 0; !rc && k * ch < dim; k++) {
+        const int slot = (int)(k & 1);
+        const int64_t i0 = k * ch, cnt = std::min<int64_t>(ch, dim - i0);
+        const void* src;
+        if (direct) {
+            src = (const double2*)s->state + i0;
+        } else {
+            void* dst = (char*)s->scratch + (size_t)(slot * ch * eb);
+            const int nb = grid_for(cnt);
+            if (c64) k_file_chunk<true><<<nb, kRThreads, 0, s->stream>>>((const float2*)s->state, mode, dim, i0, cnt, dst);
+            else k_file_chunk<false><<<nb, kRThreads, 0, s->stream>>>((const double2*)s->state, mode, dim, i0, cnt, dst);
+            src = dst;
+        }
+        rc = bs_cuda_check(s, cudaMemcpyAsync(hb[slot], src, (size_t)(cnt * eb), cudaMemcpyDeviceToHost, s->stream), "file copy");
+        if (!rc) rc = bs_cuda_check(s, cudaEventRecord(ev[slot], s->stream), "file copy");
+        if (!rc && pending >= 0) rc = flush(pending);
+        pending = k;
+    }
+    if (!rc && pending >= 0) rc = flush(pending);
+    cudaStreamSynchronize(s->stream);
+    if (std::fclose(f) != 0 && !rc) rc = bs_fail(s, BS_ERR_IO, std::string("close failed: ") + path);
+    for (int i = 0; i < 2; i++) {
+        if (hb[i]) cudaFreeHost(hb[i]);
+        if (ev[i]) cudaEventDestroy(ev[i]);
+    }
+    if (!rc && bytes_out) *bytes_out = dim * eb;
+    return rc;
 }
 
 }  // extern "C"

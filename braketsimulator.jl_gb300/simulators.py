@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import os
 from typing import Sequence
 
 import numpy as np
@@ -279,6 +280,15 @@ class AbstractSimulator:
         out = np.empty(2 * d * d, dtype=np.float64)
         self._h.call("bs_reduced_density_matrix", int(q.size), _abi.iptr(q), _abi.dptr(out))
         return out.view(np.complex128).reshape(d, d)
+
+    def write_result_file(self, what: str, path) -> int:
+        """Write ``"state"`` (state-vector simulators: 2^n complex128) or ``"probabilities"``
+        (2^n float64) from the device straight to ``path``, in the byte layout of the reference's
+        memory-mapped result values; returns the number of bytes written."""
+        code = {"state": _abi.BS_FILE_STATE, "probabilities": _abi.BS_FILE_PROBABILITIES}[what]
+        n = C.c_int64()
+        self._h.call("bs_write_result_file", code, os.fsencode(os.fspath(path)), C.byref(n))
+        return n.value
 
     def marginal_probabilities(self, targets) -> np.ndarray:
         t = np.ascontiguousarray(targets, dtype=np.int32)

@@ -28,6 +28,7 @@ extern "C" {
 #define BS_ERR_STATE         4
 #define BS_ERR_UNSUPPORTED   5
 #define BS_ERR_TIMEOUT       6
+#define BS_ERR_IO            7
 
 /* handle kinds and state precision */
 #define BS_KIND_SV           0   /* StateVectorSimulator   (src/sv_simulator.jl:6-42) */
@@ -192,6 +193,17 @@ int bs_expectation_pauli_noalloc(const void* state_dev, int kind, int n_qubits, 
  * row-major, interleaved, with output index bit r <-> the r-th smallest kept endian bit (the
  * reference's loop order before its own final permutation of unsorted targets). */
 int bs_reduced_density_matrix(bs_sim* sim, int n_keep, const int* qubits, double* out);
+
+/* Large results written from the device straight to a file, in the reference's byte layout for
+ * its memory-mapped result values (_mmap_large_result_values, src/BraketSimulator.jl:410-428:
+ * `write(io, value)` of a Vector{ComplexF64} state vector or a Vector{Float64} probability
+ * vector).  what = BS_FILE_STATE (state-vector simulators: 2^n complex128, interleaved) or
+ * BS_FILE_PROBABILITIES (2^n float64; the diagonal for a density matrix).  Streams through two
+ * 32 MiB pinned buffers; bytes_out (may be null) gets the file size.  BS_ERR_IO when the file
+ * cannot be opened or written. */
+#define BS_FILE_STATE          0
+#define BS_FILE_PROBABILITIES  1
+int bs_write_result_file(bs_sim* sim, int what, const char* path, int64_t* bytes_out);
 
 /* ---- batched simulate (src/BraketSimulator.jl:347-395): n_circuits independent circuits, each
  * from |0...0> on n_qubits[c] qubits with ops[c][0..n_ops[c]).  Returns per circuit n_terms Pauli

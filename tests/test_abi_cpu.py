@@ -128,3 +128,5 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu_call():
     assert L.bs_set_tuning(None, 0, 1.0) != 0
     assert L.bs_get_tuning(None, 0, C.byref(v)) != 0
     assert L.bs_reduced_density_matrix(None, 1, None, None) != 0
+    n = C.c_int64()
+    assert L.bs_write_result_file(None, 0, b"/dev/null", C.byref(n)) != 0

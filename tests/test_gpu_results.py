@@ -234,3 +234,62 @@ def test_device_partial_trace_rejects_bad_qubits():
         with pytest.raises(bs._abi.BraketGB300Error):
             sim.reduced_density_matrix(bad)
     assert np.allclose(sim.reduced_density_matrix([0]), [[1, 0], [0, 0]])   # the handle stays usable
+
+
+def test_simulate_circuit_with_basis_rotations():
+    """Sampling X, Y, Z eigenstates after the reference's basis rotations gives fixed outcomes."""
+    O = bs.observables
+    ixs = [bs.Instruction(bs.H(), [0]), bs.Instruction(bs.H(), [1]), bs.Instruction(bs.S(), [1]),
+           bs.Instruction(bs.X(), [2])]
+    c = bs.Circuit(ixs, [bs.Sample(O.X(), (0,)), bs.Sample(O.Y(), (1,)), bs.Sample(O.Z(), (2,))])
+    for sim in (bs.StateVectorSimulator(3, 0), bs.DensityMatrixSimulator(3, 0)):
+        res = bs.simulate(sim, c.to_program(200), 200, seed=1)
+        m = res["measurements"]
+        assert m.shape == (200, 3)
+        assert (m[:, 0] == 0).all() and (m[:, 1] == 0).all() and (m[:, 2] == 1).all()
+
+
+@pytest.mark.parametrize("precision", ["c128", "c64"])
+def test_result_files_match_host_results(tmp_path, precision):
+    """bs_write_result_file streams the state and probability vectors to files whose bytes are the
+    host results' bytes (complex128 / float64, as the reference writes them)."""
+    n = 12
+    sim = bs.StateVectorSimulator(n, 0, precision=precision)
+    sim.evolve(random_circuit(n, 60, np.random.default_rng(31)))
+    sv, pr = sim.state_vector, sim.probabilities()
+    assert sim.write_result_file("state", tmp_path / "sv.bin") == sv.nbytes
+    assert sim.write_result_file("probabilities", tmp_path / "p.bin") == pr.nbytes
+    assert (tmp_path / "sv.bin").read_bytes() == np.ascontiguousarray(sv, dtype=np.complex128).tobytes()
+    assert (tmp_path / "p.bin").read_bytes() == pr.tobytes()
+    dm = bs.DensityMatrixSimulator(5, 0, precision=precision)
+    dm.evolve(random_circuit(5, 30, np.random.default_rng(32)))
+    assert dm.write_result_file("probabilities", tmp_path / "d.bin") == 8 * 32
+    assert (tmp_path / "d.bin").read_bytes() == dm.probabilities().tobytes()
+    with pytest.raises(bs._abi.BraketGB300Error):
+        dm.write_result_file("state", tmp_path / "x.bin")
+    with pytest.raises(bs._abi.BraketGB300Error) as e:
+        sim.write_result_file("state", tmp_path / "missing-dir" / "x.bin")
+    assert e.value.code == bs._abi.BS_ERR_IO
+
+
+def test_simulate_writes_large_results_to_files(tmp_path):
+    """simulate(..., mmap_threshold) leaves values above the threshold empty and returns their files
+    (the reference's mmap convention for external callers)."""
+    n = 17   # state 2 MiB (to a file), probabilities 1 MiB (kept: not above 1 MiB)
+    prog = bs.Program(random_circuit(n, 40, np.random.default_rng(33)), [bs.StateVector(), bs.Probability(()), bs.Probability((0, 1))])
+    ref = bs.simulate(bs.StateVectorSimulator(n, 0), prog, 0)
+    out = bs.simulate(bs.StateVectorSimulator(n, 0), prog, 0, mmap_threshold=bs.program.MMAP_THRESHOLD,
+                      mmap_dir=tmp_path)
+    assert out["mmapLengths"] == (1 << n,)
+    (path,) = out["mmapPaths"]
+    got = np.frombuffer(open(path, "rb").read(), dtype=np.complex128)
+    assert np.array_equal(got, ref["resultTypes"][0][1])
+    assert out["resultTypes"][0][1].size == 0
+    assert np.array_equal(out["resultTypes"][1][1], ref["resultTypes"][1][1])
+    assert np.array_equal(out["resultTypes"][2][1], ref["resultTypes"][2][1])
+    # threshold 0: every value goes to a file, the small marginal from the host
+    out0 = bs.simulate(bs.StateVectorSimulator(n, 0), prog, 0, mmap_threshold=0, mmap_dir=tmp_path)
+    assert out0["mmapLengths"] == (1 << n, 1 << n, 4)
+    for (rt, v), p, r in zip(out0["resultTypes"], out0["mmapPaths"], ref["resultTypes"]):
+        assert v.size == 0
+        assert open(p, "rb").read() == np.asarray(r[1]).tobytes()
