@@ -53,6 +53,37 @@ void bs_arena_release(bs_sim* s) {
     s->arena_used = 0;
 }
 
+namespace {
+// Pinned landing buffer for small device-to-host results, one per host thread (handles are used
+// from one thread at a time; several handles on one thread copy one after another).
+constexpr size_t kOutStage = (size_t)1 << 20;
+struct OutStage {
+    void* p = nullptr;
+    ~OutStage() {
+        if (p) cudaFreeHost(p);
+    }
+};
+thread_local OutStage t_out;
+}  // namespace
+
+int bs_copy_out(bs_sim* s, void* host, const void* dev, size_t bytes, const char* what) {
+    if (s->capturing)   // the graph owner's buffer: enqueue only
+        return bs_cuda_check(s, cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, s->stream), what);
+    if (bytes <= kOutStage && !t_out.p && cudaMallocHost(&t_out.p, kOutStage) != cudaSuccess) {
+        cudaGetLastError();
+        t_out.p = nullptr;
+    }
+    if (bytes <= kOutStage && t_out.p) {
+        int rc = bs_cuda_check(s, cudaMemcpyAsync(t_out.p, dev, bytes, cudaMemcpyDeviceToHost, s->stream), what);
+        if (!rc) rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), what);
+        if (!rc) std::memcpy(host, t_out.p, bytes);
+        return rc;
+    }
+    int rc = bs_cuda_check(s, cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, s->stream), what);
+    if (!rc) rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), what);
+    return rc;
+}
+
 int bs_ensure_scratch(bs_sim* s, int64_t bytes) {
     if (s->scratch_bytes >= bytes) return BS_OK;
     if (s->capturing) return bs_fail(s, BS_ERR_STATE, "scratch growth during graph capture");
@@ -312,6 +343,11 @@ int bs_state_device_ptr(bs_sim* s, void** out) {
 int bs_last_stats(const bs_sim* s, bs_stats* out) {
     if (!s || !out) return BS_ERR_INVALID_ARG;
     *out = s->stats;
+    if (s->stats_pending) {   // an evolve that returned without waiting: its device time
+        float ms = 0.f;
+        if (cudaEventSynchronize(s->ev1) == cudaSuccess && cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess)
+            out->gpu_ms = ms;
+    }
     return BS_OK;
 }
 
@@ -368,6 +404,7 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     if (!s) return BS_ERR_INVALID_ARG;
     if (n_ops < 0 || (n_ops > 0 && !ops)) return bs_fail(s, BS_ERR_INVALID_ARG, "bad op list");
     s->stats = bs_stats{};
+    s->stats_pending = false;
     if (!s->defer_sync) s->tc_events_used = 0;   // deferred evolves keep their launch events for the caller
     s->alias_valid = false;
     if (!s->capturing) cudaEventRecord(s->ev0, s->stream);
@@ -459,6 +496,12 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     if (rc) return rc;
     if (s->capturing || s->defer_sync) return BS_OK;   // the graph's launcher / the caller synchronises and checks
     cudaEventRecord(s->ev1, s->stream);
+    if (!s->flag_armed && s->tc_events_used == 0) {
+        // nothing to check on the device: return without waiting (the next result read synchronises;
+        // bs_last_stats waits for the end event when asked for the time)
+        s->stats_pending = true;
+        return bs_cuda_check(s, cudaGetLastError(), "evolve");
+    }
     rc = bs_cuda_check(s, cudaEventSynchronize(s->ev1), "evolve");
     if (rc) return rc;
     float ms = 0;

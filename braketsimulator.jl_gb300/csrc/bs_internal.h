@@ -119,6 +119,7 @@ struct bs_sim {
     // graph (the graph's copy nodes read it on every replay).
     bool capturing = false;
     bool defer_sync = false;   // bs_evolve returns without synchronising (an internal caller syncs later)
+    bool stats_pending = false;   // an evolve returned before its end event (ev1) completed
     std::vector<std::pair<char*, size_t>> arena;   // chunks (pointer, capacity)
     size_t arena_used = 0;                          // bytes used in the last chunk
 };
@@ -126,6 +127,9 @@ struct bs_sim {
 // ---- helpers implemented in bs_api.cu
 int bs_fail(bs_sim* s, int code, const std::string& msg);
 int bs_cuda_check(bs_sim* s, cudaError_t e, const char* what);
+// Device-to-host copy of a result, stream synchronised; small ones land in a pinned per-thread
+// buffer first (a pageable copy takes a staged driver path).  During graph capture: enqueue only.
+int bs_copy_out(bs_sim* s, void* host, const void* dev, size_t bytes, const char* what);
 int bs_ensure_scratch(bs_sim* s, int64_t bytes);
 int bs_ensure_plan(bs_sim* s, int64_t bytes);
 // Pinned host region for one upload of `bytes`; call bs_stage_done after queuing the copy.

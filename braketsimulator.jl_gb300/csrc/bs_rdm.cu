@@ -197,7 +197,5 @@ extern "C" int bs_reduced_density_matrix(bs_sim* s, int n_keep, const int* qubit
     k_rdm_reduce<<<(unsigned)std::min<int64_t>((D * D + 255) / 256, 152 * 8), 256, 0, s->stream>>>(partial, d, (int)chunks, dout);
     rc = bs_cuda_check(s, cudaGetLastError(), "reduced density matrix");
     if (rc) return rc;
-    rc = bs_cuda_check(s, cudaMemcpyAsync(out, dout, (size_t)obytes, cudaMemcpyDeviceToHost, s->stream), "reduced density matrix");
-    if (rc) return rc;
-    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "reduced density matrix sync");
+    return bs_copy_out(s, out, dout, (size_t)obytes, "reduced density matrix");
 }

@@ -269,9 +269,7 @@ int bs_probabilities(bs_sim* s, double* host_out, int64_t n) {
         if (c64) k_prob_dm<true><<<grid_for(dim), kRThreads, 0, s->stream>>>((const float2*)s->state, d, dim);
         else k_prob_dm<false><<<grid_for(dim), kRThreads, 0, s->stream>>>((const double2*)s->state, d, dim);
     }
-    rc = bs_cuda_check(s, cudaMemcpyAsync(host_out, d, (size_t)dim * 8, cudaMemcpyDeviceToHost, s->stream), "probabilities");
-    if (rc) return rc;
-    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "probabilities sync");
+    return bs_copy_out(s, host_out, d, (size_t)dim * 8, "probabilities");
 }
 
 int bs_expectation_pauli(bs_sim* s, int n_terms, const uint64_t* xmask, const uint64_t* zmask, const double* coeffs,
@@ -323,15 +321,10 @@ int bs_expectation_pauli(bs_sim* s, int n_terms, const uint64_t* xmask, const ui
         }
     }
     k_sum_partials<<<n_terms, 256, 0, s->stream>>>(partial, nb, n_terms, res);
-    rc = bs_cuda_check(s, cudaMemcpyAsync(out, res, (size_t)n_terms * 8, cudaMemcpyDeviceToHost, s->stream), "expectation");
-    if (rc) return rc;
-    if (s->capturing) {
-        // out is the graph owner's pinned buffer, filled on every replay
-        if (coeffs) return bs_fail(s, BS_ERR_INVALID_ARG, "coefficients are applied after a captured graph runs");
-        return BS_OK;
-    }
-    rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "expectation sync");
-    if (rc) return rc;
+    if (s->capturing && coeffs) return bs_fail(s, BS_ERR_INVALID_ARG, "coefficients are applied after a captured graph runs");
+    // during capture out is the graph owner's pinned buffer, filled on every replay
+    rc = bs_copy_out(s, out, res, (size_t)n_terms * 8, "expectation");
+    if (rc || s->capturing) return rc;
     if (coeffs)
         for (int t = 0; t < n_terms; t++) out[t] *= coeffs[t];
     return BS_OK;
@@ -373,9 +366,7 @@ int bs_expectation_matrix(bs_sim* s, const double* matrix, int k, const int* tar
     else
         k_matrix_expect<false><<<nb, kRThreads, 0, s->stream>>>((const double2*)s->state, s->n, k, d_eb, d_o, dm, partial);
     k_sum_partials<<<1, 256, 0, s->stream>>>(partial, nb, 1, partial + nb);
-    rc = bs_cuda_check(s, cudaMemcpyAsync(out, partial + nb, 8, cudaMemcpyDeviceToHost, s->stream), "expectation");
-    if (rc) return rc;
-    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "expectation sync");
+    return bs_copy_out(s, out, partial + nb, 8, "expectation");
 }
 
 int bs_marginal_probabilities(bs_sim* s, int k, const int* targets, double* host_out) {
@@ -406,9 +397,7 @@ int bs_marginal_probabilities(bs_sim* s, int k, const int* targets, double* host
     else
         k_marginal<false><<<nb, kRThreads, (size_t)D * 8, s->stream>>>((const double2*)s->state, dm, s->n, k, (const int*)s->plan_buf, partial);
     k_sum_partials<<<D, 256, 0, s->stream>>>(partial, nb, D, partial + (int64_t)nb * D);
-    rc = bs_cuda_check(s, cudaMemcpyAsync(host_out, partial + (int64_t)nb * D, (size_t)D * 8, cudaMemcpyDeviceToHost, s->stream), "marginal");
-    if (rc) return rc;
-    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "marginal sync");
+    return bs_copy_out(s, host_out, partial + (int64_t)nb * D, (size_t)D * 8, "marginal");
 }
 
 // Large results straight from the device to a file (the reference writes result values above

@@ -47,15 +47,17 @@ __device__ __forceinline__ void ff_warp_sum(ffsum& a) {
     }
 }
 
-// Per block of kBlk probabilities: its float-float sum (bsum) and the inclusive prefix sums of its
-// kCpb chunks relative to the block start (cinc[b * kCpb + c]).  128 threads; warp w sums chunks
-// w, w + 4, ... with coalesced reads, warp 0 scans the chunk sums.
-__global__ void __launch_bounds__(128) k_block_sums(const double2* __restrict__ st, int dm, int64_t dim,
-                                                    double* __restrict__ bsum, double* __restrict__ cinc) {
-    __shared__ float ch[kCpb], cl[kCpb];
-    const int64_t b = blockIdx.x;
+// Per block of kBlk probabilities: its float-float sum (*bsum) and the inclusive prefix sums of its
+// kCpb chunks relative to the block start (cinc[c]).  128 threads; warp w sums chunks w, w + 4, ...
+// with coalesced reads, warp 0 scans the chunk sums.  Ends with a barrier.
+__device__ __forceinline__ void block_chunk_sums(const double2* __restrict__ st, int dm, int64_t dim, int64_t b,
+                                                 float* ch, float* cl, double* bsum, double* cinc) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int c = warp; c < kCpb; c += 4) {
+        if (b * kBlk + (int64_t)c * kChunk >= dim) {   // past the end: an empty chunk sums to zero
+            if (lane == 0) { ch[c] = 0.f; cl[c] = 0.f; }
+            continue;
+        }
         const int64_t i = b * kBlk + (int64_t)c * kChunk + lane;
         ffsum a{0.f, 0.f};
         if (i < dim) {
@@ -67,30 +69,39 @@ __global__ void __launch_bounds__(128) k_block_sums(const double2* __restrict__ 
         if (lane == 0) { ch[c] = a.h; cl[c] = a.l; }
     }
     __syncthreads();
-    if (warp != 0) return;
-    // lane holds chunks 4 lane .. 4 lane + 3: local inclusive sums, then a warp scan of the totals
-    ffsum loc[4];
-    ffsum run{0.f, 0.f};
+    if (warp == 0) {
+        // lane holds chunks 4 lane .. 4 lane + 3: local inclusive sums, then a warp scan of the totals
+        ffsum loc[4];
+        ffsum run{0.f, 0.f};
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-        fsum_add(run, ch[4 * lane + k], cl[4 * lane + k]);
-        loc[k] = run;
-    }
-    ffsum pre = run;   // inclusive scan of the lane totals
+        for (int k = 0; k < 4; k++) {
+            fsum_add(run, ch[4 * lane + k], cl[4 * lane + k]);
+            loc[k] = run;
+        }
+        ffsum pre = run;   // inclusive scan of the lane totals
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const float h = __shfl_up_sync(0xffffffffu, pre.h, o), l = __shfl_up_sync(0xffffffffu, pre.l, o);
-        if (lane >= o) fsum_add(pre, h, l);
-    }
-    ffsum off{__shfl_up_sync(0xffffffffu, pre.h, 1), __shfl_up_sync(0xffffffffu, pre.l, 1)};
-    if (lane == 0) off = ffsum{0.f, 0.f};
+        for (int o = 1; o < 32; o <<= 1) {
+            const float h = __shfl_up_sync(0xffffffffu, pre.h, o), l = __shfl_up_sync(0xffffffffu, pre.l, o);
+            if (lane >= o) fsum_add(pre, h, l);
+        }
+        ffsum off{__shfl_up_sync(0xffffffffu, pre.h, 1), __shfl_up_sync(0xffffffffu, pre.l, 1)};
+        if (lane == 0) off = ffsum{0.f, 0.f};
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-        ffsum v = off;
-        fsum_add(v, loc[k].h, loc[k].l);
-        cinc[b * kCpb + 4 * lane + k] = ff2d(v.h, v.l);
+        for (int k = 0; k < 4; k++) {
+            ffsum v = off;
+            fsum_add(v, loc[k].h, loc[k].l);
+            cinc[4 * lane + k] = ff2d(v.h, v.l);
+        }
+        if (lane == 31) *bsum = ff2d(pre.h, pre.l);
     }
-    if (lane == 31) bsum[b] = ff2d(pre.h, pre.l);
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(128) k_block_sums(const double2* __restrict__ st, int dm, int64_t dim,
+                                                    double* __restrict__ bsum, double* __restrict__ cinc) {
+    __shared__ float ch[kCpb], cl[kCpb];
+    const int64_t b = blockIdx.x;
+    block_chunk_sums(st, dm, dim, b, ch, cl, bsum + b, cinc + b * kCpb);
 }
 
 // inclusive prefix of the block sums, one CTA of 1024 threads (nb is at most 2^22): a serial sum
@@ -189,6 +200,24 @@ __global__ void k_sample_rng(const double2* __restrict__ st, int dm, int64_t dim
         const uint64_t r = splitmix64(seed ^ splitmix64((uint64_t)s));
         const double u = (double)(r >> 11) * 0x1.0p-53;
         const int64_t v = cdf_find_warp(st, dm, dim, incl, cinc, nb, u * incl[nb - 1]);
+        if ((threadIdx.x & 31) == 0) out[s] = v;
+    }
+}
+
+// States of at most one CDF block (dim <= kBlk): every CTA forms the block's chunk prefix sums in
+// shared memory itself (the arithmetic of k_block_sums, so the same CDF), then its warps draw their
+// shots as k_sample_rng does.  One launch instead of three.
+__global__ void __launch_bounds__(128) k_sample_small(const double2* __restrict__ st, int dm, int64_t dim,
+                                                      uint64_t seed, int64_t shots, int64_t* __restrict__ out) {
+    __shared__ float ch[kCpb], cl[kCpb];
+    __shared__ double s_cinc[kCpb], s_total;
+    block_chunk_sums(st, dm, dim, 0, ch, cl, &s_total, s_cinc);
+    const double total = 0.0 + s_total;   // the block-prefix scan's value for one block
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; s < shots; s += warps) {
+        const uint64_t r = splitmix64(seed ^ splitmix64((uint64_t)s));
+        const double u = (double)(r >> 11) * 0x1.0p-53;
+        const int64_t v = cdf_find_warp(st, dm, dim, &s_total, s_cinc, 1, u * total);   // nb = 1: incl unread
         if ((threadIdx.x & 31) == 0) out[s] = v;
     }
 }
@@ -311,9 +340,7 @@ int bs_alias_build(bs_sim* s, double wsum, unsigned flags) {
         int64_t nb = 0;
         rc = build_cdf(s, &incl, nullptr, &nb);
         if (rc) return rc;
-        rc = bs_cuda_check(s, cudaMemcpyAsync(&wsum, incl + nb - 1, 8, cudaMemcpyDeviceToHost, s->stream), "weight sum");
-        if (rc) return rc;
-        rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "weight sum sync");
+        rc = bs_copy_out(s, &wsum, incl + nb - 1, 8, "weight sum");
         if (rc) return rc;
         if (!(wsum > 0.0)) return bs_fail(s, BS_ERR_STATE, "state has zero norm");
     }
@@ -387,27 +414,37 @@ int bs_sample_direct(bs_sim* s, const double* u, int64_t shots, double wsum, int
     const int64_t dim = (int64_t)1 << s->n;
     k_sample_direct<<<grid(shots, 128), 128, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, incl, nb,
                                                                du, wsum, shots, dout);
-    cudaMemcpyAsync(out, dout, (size_t)shots * 8, cudaMemcpyDeviceToHost, s->stream);
-    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "sample direct");
+    return bs_copy_out(s, out, dout, (size_t)shots * 8, "sample direct");
 }
 
 int bs_sample(bs_sim* s, uint64_t seed, int64_t shots, int64_t* out) {
     if (!s) return BS_ERR_INVALID_ARG;
     if (shots < 0 || (shots > 0 && !out)) return bs_fail(s, BS_ERR_INVALID_ARG, "bad shot buffer");
     if (shots == 0) return BS_OK;
-    double* incl = nullptr;
-    double* cinc = nullptr;
-    int64_t nb = 0;
-    void* buf = nullptr;
-    int rc = build_cdf(s, &incl, &cinc, &nb, shots * 8, &buf);
-    if (rc) return rc;
-    int64_t* dout = (int64_t*)buf;
     const int64_t dim = (int64_t)1 << s->n;
-    k_sample_rng<<<grid(shots * 32, 128), 128, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, incl, cinc, nb,
-                                                            seed, shots, dout);
-    cudaMemcpyAsync(out, dout, (size_t)shots * 8, cudaMemcpyDeviceToHost, s->stream);
-    if (s->capturing) return bs_cuda_check(s, cudaGetLastError(), "sample");   // out: the graph owner's pinned buffer
-    return bs_cuda_check(s, cudaStreamSynchronize(s->stream), "sample");
+    const int mode = (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0);
+    int64_t* dout;
+    int rc;
+    if (dim <= kBlk) {
+        rc = bs_ensure_scratch(s, shots * 8);
+        if (rc) return rc;
+        dout = (int64_t*)s->scratch;
+        const unsigned g = (unsigned)std::min<int64_t>(152, std::max<int64_t>(1, (shots + 15) / 16));
+        k_sample_small<<<g, 128, 0, s->stream>>>((const double2*)s->state, mode, dim, seed, shots, dout);
+    } else {
+        double* incl = nullptr;
+        double* cinc = nullptr;
+        int64_t nb = 0;
+        void* buf = nullptr;
+        rc = build_cdf(s, &incl, &cinc, &nb, shots * 8, &buf);
+        if (rc) return rc;
+        dout = (int64_t*)buf;
+        k_sample_rng<<<grid(shots * 32, 128), 128, 0, s->stream>>>((const double2*)s->state, mode, dim, incl, cinc, nb,
+                                                                seed, shots, dout);
+    }
+    rc = bs_cuda_check(s, cudaGetLastError(), "sample");
+    if (rc) return rc;
+    return bs_copy_out(s, out, dout, (size_t)shots * 8, "sample");   // capture: out is the graph owner's pinned buffer
 }
 
 }  // extern "C"

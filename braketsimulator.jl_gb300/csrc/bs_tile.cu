@@ -1668,9 +1668,7 @@ int bs_check_device_flag(bs_sim* s) {
     if (!s->flag_armed) return BS_OK;
     s->flag_armed = false;
     int flag = 0;
-    int rc = bs_cuda_check(s, cudaMemcpyAsync(&flag, s->dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
-                           "flag read");
-    if (!rc) rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "flag read");
+    const int rc = bs_copy_out(s, &flag, s->dev_flag, sizeof(int), "flag read");
     if (rc) return rc;
     if (flag) return bs_fail(s, BS_ERR_TIMEOUT, "a tensor-core sweep gave up waiting for its copies or MMAs");
     return BS_OK;

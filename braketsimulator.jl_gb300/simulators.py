@@ -40,12 +40,13 @@ class Instruction:
 
 def _ops_for(instructions, dm: bool, noise_mode: int):
     """Lower instructions into a bs_op array; returns (array, keepalive buffers)."""
-    ops = []
+    ops = []    # the bs_op structs as bytes, joined into one array below
     keep = []
+    skip = (Measure, Reset, Barrier, Delay)
     for ix in instructions:
         op = ix.operator
         t = ix.target
-        if isinstance(op, (Measure, Reset, Barrier, Delay)):
+        if isinstance(op, skip):
             continue
         if isinstance(op, Noise):
             if not dm:
@@ -62,15 +63,18 @@ def _ops_for(instructions, dm: bool, noise_mode: int):
                 o.targets[j] = q
             o.n_matrices = len(ln.matrices)
             o.matrix = _abi.dptr(buf)
-            ops.append(o)
+            ops.append(bytes(o))
             continue
         if not isinstance(op, Gate):
             raise TypeError(f"cannot apply {op!r}")
         for o, buf in _gate_ops(op, t):
             keep.append(buf)
             ops.append(o)
-    arr = (_abi.BsOp * max(1, len(ops)))(*ops)
-    return arr, len(ops), keep
+    n = len(ops)
+    if n == 0:
+        return (_abi.BsOp * 1)(), 0, keep
+    arr = (_abi.BsOp * n).from_buffer_copy(b"".join(ops))
+    return arr, n, keep
 
 
 # Lowered engine ops of fixed gates, keyed by (gate type, angles, pow_exponent, targets).  Gates
@@ -81,9 +85,10 @@ _LOWER_CACHE_MAX = 1 << 16
 
 
 def _gate_ops(op, t):
+    """[(bs_op struct bytes, matrix buffer)] for one gate on targets t (a tuple of ints)."""
     key = None
     if not isinstance(op, (Unitary, Control)):
-        key = (type(op), op.angle, op.pow_exponent, tuple(int(q) for q in t))
+        key = (type(op), op.angle, op.pow_exponent, t)
         hit = _LOWER_CACHE.get(key)
         if hit is not None:
             return hit
@@ -103,7 +108,7 @@ def _gate_ops(op, t):
             o.controls[j] = q
             o.control_values[j] = v
         o.matrix = _abi.dptr(buf)
-        res.append((o, buf))
+        res.append((bytes(o), buf))
     if key is not None:
         if len(_LOWER_CACHE) >= _LOWER_CACHE_MAX:
             _LOWER_CACHE.clear()

@@ -293,3 +293,28 @@ def test_simulate_writes_large_results_to_files(tmp_path):
     for (rt, v), p, r in zip(out0["resultTypes"], out0["mmapPaths"], ref["resultTypes"]):
         assert v.size == 0
         assert open(p, "rb").read() == np.asarray(r[1]).tobytes()
+
+
+def _splitmix64(x):
+    m = (1 << 64) - 1
+    x = (x + 0x9E3779B97F4A7C15) & m
+    x = ((x ^ (x >> 30)) * 0xBF58476D1CE4E5B9) & m
+    x = ((x ^ (x >> 27)) * 0x94D049BB133111EB) & m
+    return x ^ (x >> 31)
+
+
+@pytest.mark.parametrize("kind,n", [("sv", 10), ("sv", 14), ("dm", 5), ("dm", 7)])
+def test_own_rng_samples_follow_the_inverse_cdf(kind, n):
+    """bs_sample draws u_s = splitmix64(seed ^ splitmix64(s)) / 2^64 and returns the first index whose
+    running probability sum reaches u_s * total: the one-launch path for states of one CDF block
+    (2^n <= 4096) and the three-kernel path agree with the host inverse CDF (ties aside)."""
+    shots, seed = 3000, 12345
+    rng = np.random.default_rng(n)
+    sim = bs.StateVectorSimulator(n, shots) if kind == "sv" else bs.DensityMatrixSimulator(n, shots)
+    sim.evolve(random_circuit(n, 40, rng))
+    p = sim.probabilities()
+    c = np.cumsum(p)
+    u = np.array([(_splitmix64(seed ^ _splitmix64(s)) >> 11) * 2.0 ** -53 for s in range(shots)])
+    want = np.minimum(np.searchsorted(c, u * c[-1], side="left"), p.size - 1)
+    got = sim.samples(seed=seed)
+    assert np.mean(got == want) > 0.999
