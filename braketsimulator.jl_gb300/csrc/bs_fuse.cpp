@@ -270,6 +270,107 @@ void bs_fuse_tc(const std::vector<HostGate>& in, const int* local, int T, double
     for (Block& b : open) emit(b);
 }
 
+// Fusion for the sweeps that run on the CUDA cores (float-float and complex64 tile kernels): runs of
+// gates whose tile bits (targets and controls) fit in maxk bits become one dense maxk-bit gate when
+// that is cheaper, counting one shared-memory pass of the tile (pass, in units of a dense 1-qubit
+// gate's arithmetic) per gate applied.  The kernels apply every gate as one pass, so fusing two
+// 1-qubit gates on different bits into a 4x4 keeps the arithmetic and halves the passes.  Gates with
+// bits outside the tile, 3+-bit gates and channels stay as they are and close the blocks they touch.
+void bs_fuse_small(const std::vector<HostGate>& in, const int* local, double pass, int maxk, std::vector<HostGate>& out) {
+    out.clear();
+    struct SBlock {
+        uint64_t bits = 0;
+        std::vector<int> idx;
+        double cost = 0;
+    };
+    std::vector<SBlock> open;
+    auto gate_bits = [&](const HostGate& g, bool& in_tile) {
+        uint64_t b = g.cmask;
+        for (int q = 0; q < g.k; q++) b |= 1ULL << g.ebit[q];
+        in_tile = true;
+        for (uint64_t r = b; r; r &= r - 1)
+            if (local[__builtin_ctzll(r)] < 0) in_tile = false;
+        return b;
+    };
+    auto emit = [&](SBlock& b) {
+        const int k = __builtin_popcountll(b.bits);
+        if (b.idx.size() < 2 || pass + (double)(1 << k) / 2.0 >= b.cost) {
+            for (int i : b.idx) out.push_back(in[(size_t)i]);
+            return;
+        }
+        // the block's bits take block positions 0..k-1; the 32x32 product then holds U (x) I
+        int pos[64];
+        for (int e = 0; e < 64; e++) pos[e] = -1;
+        HostGate f;
+        f.kind = 0;
+        f.k = k;
+        int q = 0;
+        for (int e = 0; e < 64; e++)
+            if ((b.bits >> e) & 1ULL) { pos[e] = q; f.ebit[q] = e; q++; }
+        std::vector<cd> U(32 * 32, cd(0, 0));
+        for (int r = 0; r < 32; r++) U[(size_t)r * 33] = 1;
+        for (int i : b.idx) apply_block(in[(size_t)i], pos, 0, U.data());
+        const int D = 1 << k;
+        f.mat.assign((size_t)2 * D * D, 0.0);
+        for (int r = 0; r < D; r++)
+            for (int c = 0; c < D; c++) {
+                f.mat[(size_t)2 * (r * D + c)] = U[(size_t)r * 32 + c].real();
+                f.mat[(size_t)2 * (r * D + c) + 1] = U[(size_t)r * 32 + c].imag();
+            }
+        out.push_back(std::move(f));
+    };
+    auto close_touching = [&](uint64_t bits) {
+        for (size_t j = 0; j < open.size();) {
+            if (open[j].bits & bits) {
+                emit(open[j]);
+                open.erase(open.begin() + (long)j);
+            } else {
+                j++;
+            }
+        }
+    };
+    for (size_t i = 0; i < in.size(); i++) {
+        const HostGate& g = in[i];
+        if (g.kind == 5) {   // a reference-rule channel commutes with nothing
+            for (SBlock& b : open) emit(b);
+            open.clear();
+            out.push_back(g);
+            continue;
+        }
+        bool in_tile = false;
+        const uint64_t bits = gate_bits(g, in_tile);
+        const bool fusable = g.kind <= 2 && in_tile && bits && __builtin_popcountll(bits) <= maxk;
+        if (!fusable) {
+            close_touching(bits);
+            out.push_back(g);
+            continue;
+        }
+        uint64_t uni = bits;
+        for (const SBlock& b : open) if (b.bits & bits) uni |= b.bits;
+        if (__builtin_popcountll(uni) > maxk) {
+            close_touching(bits);
+            uni = bits;
+        }
+        SBlock nb;
+        nb.bits = uni;
+        // merge the intersecting blocks (pairwise disjoint, so their gates commute), then the gate
+        for (size_t j = 0; j < open.size();) {
+            if (open[j].bits & bits) {
+                nb.idx.insert(nb.idx.end(), open[j].idx.begin(), open[j].idx.end());
+                nb.cost += open[j].cost;
+                open.erase(open.begin() + (long)j);
+            } else {
+                j++;
+            }
+        }
+        std::sort(nb.idx.begin(), nb.idx.end());
+        nb.idx.push_back((int)i);
+        nb.cost += is_plain_cz(g) ? 0.1 : pass + ff_cost(g);   // CZs share one parity pass anyway
+        open.push_back(std::move(nb));
+    }
+    for (SBlock& b : open) emit(b);
+}
+
 bool bs_tc_exponent(const double* mat, int n_mat, int& eu) {
     double mx = 0;
     for (size_t i = 0; i < (size_t)n_mat * 2048; i++) {

@@ -159,6 +159,7 @@ double bs_tc_cost(const bs_sim* s);
 // Fold runs of in-tile gates into kind-4 HostGates (5 endian bits, 32x32 matrix) where that is cheaper
 // (float-float cost above `threshold`).  local[e]: tile position of endian bit e or -1.
 void bs_fuse_tc(const std::vector<HostGate>& in, const int* local, int T, double threshold, std::vector<HostGate>& out);
+void bs_fuse_small(const std::vector<HostGate>& in, const int* local, double pass, int maxk, std::vector<HostGate>& out);
 // Smallest eu with every entry of the n_mat 32x32 matrices below 2^eu; false if not finite or above 2^12.
 bool bs_tc_exponent(const double* mat, int n_mat, int& eu);
 

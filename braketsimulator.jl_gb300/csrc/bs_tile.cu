@@ -1348,8 +1348,19 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         for (int b = 0; b < 64; b++) local[b] = -1;
         for (int b = 0; b < L; b++) local[b] = b;
         for (size_t i = 0; i < sw.hi_bits.size(); i++) local[sw.hi_bits[i]] = L + (int)i;
-        std::vector<HostGate> merged;
-        merge_diagonals((use_tc && fused_ok[si]) ? fused_all[si] : sw.gates, merged);
+        std::vector<HostGate> merged, small;
+        if (use_tc && fused_ok[si]) {
+            merge_diagonals(fused_all[si], merged);
+        } else if (c64) {
+            // complex64 sweep: 1- and 2-bit runs fused into dense 2-bit gates where that saves passes (a
+            // pass of the complex64 kernel costs about four 1-qubit gates' arithmetic; batch of 512
+            // circuits 1.79 -> 1.48 s on the device).  The float-float kernel is bound by its
+            // arithmetic: fusing there measured slower (18 qubits: 7.7 -> 9.2 ms)
+            bs_fuse_small(sw.gates, local, 4.0, 2, small);
+            merge_diagonals(small, merged);
+        } else {
+            merge_diagonals(sw.gates, merged);
+        }
         const std::vector<HostGate>* glist = &merged;
         for (const HostGate& hg : *glist) {
             if (hg.kind == 5) {
