@@ -378,6 +378,18 @@ def batch_bench(bs):
                       "replay_equals_one_shot": same}}
 
 
+def max_over_ranks(vals, world, device="cuda"):
+    """The timed quantities' maximum over the replicas (one all_reduce; as is for one rank).  Each
+    rank runs its own full workload, so the whole-job rate is the units of all ranks over this time."""
+    if world <= 1:
+        return [float(v) for v in vals]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in vals], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def run_reference(args, rank, world):
     """--impl reference: the reference's CPU kernels (oracle port; Julia is not installed)
     on the host cores, bounded sample of the same workload per step."""
@@ -454,11 +466,7 @@ def main():
             tc_launches += st["tc_launches"]
         barrier()
         wall = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([wall, dev_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        wall, dev_ms = float(t[0]), float(t[1])
+    wall, dev_ms = max_over_ranks([wall, dev_ms], world)
     if rank != 0:
         return
     hbm, bf16, src = peaks()
