@@ -247,7 +247,7 @@ def adjoint_bench(bs, n=24, layers=10, terms=48, shift_params=24, seed=3):
             "param_shift_sample": f"{shift_params} of {P} parameters, 2 circuits each"}
 
 
-def ghz_bench(bs, reps=100):
+def ghz_bench(bs, reps=100, cpu=False):
     """GHZ-10 (H, CNOT(0,k)), full probabilities and 1000 shots per circuit: latency-bound."""
     import torch
     ops = [bs.Instruction(bs.H(), [0])] + [bs.Instruction(bs.CNot(), [0, k]) for k in range(1, 10)]
@@ -267,7 +267,43 @@ def ghz_bench(bs, reps=100):
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / reps
     ok = abs(p[0] - 0.5) < 1e-15 and abs(p[-1] - 0.5) < 1e-15 and set(np.unique(s)) <= {0, 1023}
-    return {"us_per_circuit": round(dt * 1e6, 1), "circuits_per_s": round(1 / dt, 1), "checked": bool(ok)}
+    out = {"us_per_circuit": round(dt * 1e6, 1), "circuits_per_s": round(1 / dt, 1), "checked": bool(ok)}
+    if cpu:
+        out["cpu_baseline"] = ghz_cpu_port(reps)
+    return out
+
+
+def ghz_cpu_port(reps=200):
+    """The same GHZ-10 flow on the oracle port of the reference's CPU kernels, one host thread:
+    H and nine CNOT sweeps, |psi|^2, the serial alias table and 1000 draws on a host stream."""
+    import oracle
+    L = oracle.lib()
+    h = oracle._cm(oracle.FIXED["h"])
+    x = oracle._cm(oracle.FIXED["x"])
+    rng = np.random.default_rng(0)
+    psi = np.zeros(1024, dtype=np.complex128)
+
+    def one():
+        psi[:] = 0
+        psi[0] = 1
+        L.orc_apply_1q(oracle._p(psi), 1024, oracle._p(h), 0)
+        for k in range(1, 10):
+            L.orc_apply_c1t1(oracle._p(psi), 1024, oracle._p(x), 1, 0, k)
+        p = np.abs(psi) ** 2
+        ap, al = oracle.alias_table(p)
+        j = rng.integers(0, 1024, 1000)
+        u = rng.random(1000)
+        return oracle.sample_alias(ap, al, j, u)
+
+    for _ in range(10):
+        one()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        s = one()
+    dt = (time.perf_counter() - t0) / reps
+    assert set(np.unique(s)) <= {0, 1023}
+    return {"us_per_circuit": round(dt * 1e6, 1), "cores": 1, "kind": "port",
+            "sample": f"{reps} circuits: the oracle's C kernels through ctypes, numpy |psi|^2 and RNG"}
 
 
 def dm_circuit(bs, n=14, depth=12, seed=5):
@@ -521,7 +557,7 @@ def main():
         line["cpu_baseline"], _ = cpu_baseline_port()
     if not args.no_adjoint:
         line["adjoint"] = adjoint_bench(bs)
-        line["ghz10"] = ghz_bench(bs)
+        line["ghz10"] = ghz_bench(bs, cpu=not args.no_cpu)
         line["dm14"] = dm_bench(bs)
         line["batch512"] = batch_bench(bs)
     print(json.dumps(line), flush=True)

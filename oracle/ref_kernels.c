@@ -27,6 +27,10 @@
 
 typedef double complex cplx;
 
+/* Threads only from 2^17 amplitudes: the reference's sweeps run in chunks of 2^16 pairs
+ * (src/gate_kernels.jl:489-537), so a small state is one chunk on one thread. */
+#define ORC_PAR_MIN ((int64_t)1 << 17)
+
 /* src/gate_kernels.jl:34-38 */
 static inline int64_t pad_bit(int64_t ix, int bit) {
     int64_t left = (ix >> bit) << bit;
@@ -54,7 +58,7 @@ void orc_apply_1q(cplx* psi, int64_t n_amps, const cplx* m, int qubit) {
     int e = nq - 1 - qubit;
     int64_t flipper = (int64_t)1 << e;
     cplx g00 = m[0], g01 = m[1], g10 = m[2], g11 = m[3];
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n_amps >= ORC_PAR_MIN)
     for (int64_t t = 0; t < n_amps / 2; t++) {
         int64_t lo = pad_bit(t, e), hi = lo + flipper;
         cplx a = psi[lo], b = psi[hi];
@@ -68,7 +72,7 @@ void orc_apply_2q(cplx* psi, int64_t n_amps, const cplx* m, int t1, int t2) {
     int nq = log2i(n_amps);
     int e1 = nq - 1 - t1, e2 = nq - 1 - t2;
     int b[2] = { e1 < e2 ? e1 : e2, e1 < e2 ? e2 : e1 };
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n_amps >= ORC_PAR_MIN)
     for (int64_t ix = 0; ix < n_amps / 4; ix++) {
         int64_t i00 = pad_bits(ix, b, 2);
         int64_t i10 = flip_bit(i00, e2);
@@ -88,7 +92,7 @@ void orc_apply_c1t1(cplx* psi, int64_t n_amps, const cplx* m, int cbit, int cont
     int ec = nq - 1 - control, et = nq - 1 - target;
     int small = ec < et ? ec : et, big = ec < et ? et : ec;
     cplx g00 = m[0], g01 = m[1], g10 = m[2], g11 = m[3];
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (n_amps >= ORC_PAR_MIN)
     for (int64_t ix = 0; ix < n_amps / 4; ix++) {
         int64_t i00 = pad_bit(pad_bit(ix, small), big);
         int64_t i10 = flip_bit(i00, ec);
