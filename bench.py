@@ -320,7 +320,7 @@ def dm_circuit(bs, n=14, depth=12, seed=5):
     return ops
 
 
-def dm_bench(bs, n=14):
+def dm_bench(bs, n=14, cpu=False):
     """Noisy density matrix, 14 qubits (4 GiB): diag + <X X X X> on qubits 0..3, both noise modes."""
     import torch
     ops = dm_circuit(bs, n)
@@ -342,7 +342,25 @@ def dm_bench(bs, n=14):
                      "sweep_GBps": round(st["bytes_moved"] / (st["gpu_ms"] * 1e-3) / 1e9, 1),
                      "trace": round(float(np.sum(diag)), 12), "x4": ex}
     out["instructions"] = len(ops)
+    if cpu:
+        out["cpu_baseline"] = dm_cpu_port(ops, n)
     return out
+
+
+def dm_cpu_port(ops, n=14, depth=12):
+    """Reference noise mode on the oracle port of the reference's CPU kernels (all host threads):
+    the first of the circuit's `depth` identical-shape layers is timed and scaled by `depth`."""
+    import oracle
+    oracle.lib()
+    layer = len(ops) // depth
+    sim = oracle.OracleDM(n)
+    sim.rho[:] = 0
+    sim.rho[0] = 1.0
+    t0 = time.perf_counter()
+    sim.evolve(ops[:layer])
+    dt = time.perf_counter() - t0
+    return {"s_per_circuit": round(dt * depth, 2), "cores": os.cpu_count(), "kind": "port",
+            "sample": f"1 of {depth} layers ({layer} instructions, {dt:.1f} s) timed, scaled by {depth}"}
 
 
 def batch_circuits(bs, nc=512, seed=7):
@@ -377,7 +395,7 @@ def batch_circuits(bs, nc=512, seed=7):
     return circuits, counts, obs
 
 
-def batch_bench(bs):
+def batch_bench(bs, cpu=False):
     import torch
     circuits, counts, obs = batch_circuits(bs)
     bs.batch_simulate(circuits[:8], counts[:8], obs[:8], shots=1000, seed=1)      # warm-up
@@ -411,7 +429,31 @@ def batch_bench(bs):
             "max_abs_err_c64_vs_c128_expectations": err,
             "graph": {"capture_s": round(t_cap, 3), "s_per_replay": round(t_rep, 3),
                       "circuits_per_s": round(len(circuits) / t_rep, 1), "device_ms": round(st2["gpu_ms"], 1),
-                      "replay_equals_one_shot": same}}
+                      "replay_equals_one_shot": same},
+            **({"cpu_baseline": batch_cpu_port(circuits, counts)} if cpu else {})}
+
+
+def batch_cpu_port(circuits, counts, budget_s=8.0):
+    """The batch's gate sweeps on the oracle port of the reference's CPU kernels (complex128, all host
+    threads; the reference has no complex64 path): circuits in batch order are evolved until the
+    budget is spent, and the whole batch's time is scaled from the sample by gate-sweep bytes."""
+    import oracle
+    oracle.lib()
+    total = sum(len(c) * 32.0 * 2 ** n for c, n in zip(circuits, counts))
+    done_bytes, t_used, k = 0.0, 0.0, 0
+    for c, n in zip(circuits, counts):
+        if t_used > budget_s or n > 24:
+            continue
+        sim = oracle.OracleSV(n)
+        t0 = time.perf_counter()
+        sim.evolve(c)
+        t_used += time.perf_counter() - t0
+        done_bytes += len(c) * 32.0 * 2 ** n
+        k += 1
+    est = total / (done_bytes / t_used)
+    return {"circuits_per_s": round(len(circuits) / est, 2), "s_per_batch": round(est, 1), "cores": os.cpu_count(),
+            "kind": "port", "sample": f"{k} circuits of <=24 qubits evolved in {t_used:.1f} s; the batch scaled by "
+                                      "gate-sweep bytes (2*16*2^n per gate); shots and expectations not included"}
 
 
 def max_over_ranks(vals, world, device="cuda"):
@@ -558,8 +600,8 @@ def main():
     if not args.no_adjoint:
         line["adjoint"] = adjoint_bench(bs)
         line["ghz10"] = ghz_bench(bs, cpu=not args.no_cpu)
-        line["dm14"] = dm_bench(bs)
-        line["batch512"] = batch_bench(bs)
+        line["dm14"] = dm_bench(bs, cpu=not args.no_cpu)
+        line["batch512"] = batch_bench(bs, cpu=not args.no_cpu)
     print(json.dumps(line), flush=True)
 
 
