@@ -372,11 +372,11 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const TileG
 #pragma unroll
     for (int a = 0; a < NA; a++) vv[a] = sm[spm ^ tsw[a]];
 #pragma unroll
-    for (int c = 0; c < NA / 2; c++) {
-        uint32_t w[6][2];
+    for (int c = 0; c < NA / 4; c++) {   // four amplitudes, then one 4-column TMEM store per digit slice
+        uint32_t w[6][4];
 #pragma unroll
-        for (int a = 0; a < 2; a++) {
-            const float4 v = vv[2 * c + a];
+        for (int a = 0; a < 4; a++) {
+            const float4 v = vv[4 * c + a];
             f2 q[6];
             digits2(mul2(pk(v.x, v.y), sc2), mul2(pk(v.z, v.w), sc2), q);
 #pragma unroll
@@ -386,7 +386,7 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const TileG
             }
         }
 #pragma unroll
-        for (int j = 0; j < 6; j++) st2(st.tmem + lane + (uint32_t)(kA0 + 32 * j + NA * h + 2 * c), w[j][0], w[j][1]);
+        for (int j = 0; j < 6; j++) st4(st.tmem + lane + (uint32_t)(kA0 + 32 * j + NA * h + 4 * c), w[j]);
     }
     wait_st();
     fence_before();
