@@ -22,6 +22,7 @@ BS_NOISE_PHYSICAL = 0x10
 BS_TUNE_TILE_BITS, BS_TUNE_TILE_THREADS, BS_TUNE_TC, BS_TUNE_TC_MIN_BITS, BS_TUNE_TC_COST = 0, 1, 2, 3, 4
 BS_TUNE_ADJ_SEGMENTS = 5
 BS_FILE_STATE, BS_FILE_PROBABILITIES = 0, 1
+BS_ERR_TIMEOUT = 6
 BS_ERR_IO = 7
 BS_MAX_TARGETS = 10
 BS_MAX_CONTROLS = 16
@@ -107,6 +108,7 @@ SIGNATURES = {
     "bs_reduced_density_matrix": (_i32, [_p, _i32, _P(_i32), _P(_f64)]),
     "bs_write_result_file": (_i32, [_p, _i32, C.c_char_p, _P(_i64)]),
     "bs_synchronize": (_i32, [_p]),
+    "bs_selftest_wait_timeout": (_i32, [_p, _f64]),
     "bs_state_device_ptr": (_i32, [_p, _P(_p)]),
 }
 

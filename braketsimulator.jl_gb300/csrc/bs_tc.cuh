@@ -62,7 +62,7 @@ __device__ __forceinline__ void mbar_init(uint32_t bar) {
 // bounded wait for the phase with the given parity; false if it did not complete in kSpin cycles.
 // Each try_wait suspends the thread until the phase completes or ~20 us pass, so waiting warps do not
 // take issue slots from the working ones.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait_for(uint32_t bar, uint32_t parity, long long limit) {
     const long long t0 = clock64();
     while (true) {
         uint32_t done;
@@ -72,9 +72,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
             : "r"(bar), "r"(parity), "r"(20000u)
             : "memory");
         if (done) return true;
-        if (clock64() - t0 > kSpin) return false;
+        if (clock64() - t0 > limit) return false;
     }
 }
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) { return mbar_wait_for(bar, parity, kSpin); }
 
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");

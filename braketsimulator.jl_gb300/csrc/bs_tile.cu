@@ -1675,6 +1675,39 @@ void bs_collect_tc_time(bs_sim* s) {
     s->tc_events_used = 0;
 }
 
+namespace {
+// A wait that nothing completes: one thread waits on a fresh mbarrier (no arrival, no copy and no MMA
+// in flight) with the tensor-core sweep's bounded wait, gives up after `limit` cycles and raises the
+// device flag, as a sweep whose copy or MMA never landed would.
+__global__ void k_wait_selftest(int* __restrict__ err, long long limit) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) tc::mbar_init(tc::su32(&bar));
+    __syncthreads();
+    if (threadIdx.x == 0 && !tc::mbar_wait_for(tc::su32(&bar), 0u, limit)) atomicExch(err, 1);
+}
+}  // namespace
+
+extern "C" int bs_selftest_wait_timeout(bs_sim* s, double seconds) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (!(seconds > 0.0) || seconds > 1.0) return bs_fail(s, BS_ERR_INVALID_ARG, "wait limit must be in (0, 1] s");
+    if (s->capturing) return bs_fail(s, BS_ERR_STATE, "not during graph capture");
+    int rc = BS_OK;
+    if (!s->dev_flag) {
+        rc = bs_cuda_check(s, cudaMalloc((void**)&s->dev_flag, 256), "flag alloc");
+        if (rc) return rc;
+    }
+    rc = bs_cuda_check(s, cudaMemsetAsync(s->dev_flag, 0, sizeof(int), s->stream), "flag reset");
+    if (rc) return rc;
+    s->flag_armed = true;
+    k_wait_selftest<<<1, 32, 0, s->stream>>>(s->dev_flag, (long long)(seconds * 2.0e9));
+    rc = bs_cuda_check(s, cudaGetLastError(), "self-test launch");
+    if (rc) return rc;
+    rc = bs_check_device_flag(s);
+    if (rc == BS_ERR_TIMEOUT) return bs_fail(s, BS_ERR_TIMEOUT, "self-test: the bounded wait gave up and raised the device flag");
+    if (rc == BS_OK) return bs_fail(s, BS_ERR_STATE, "self-test: the wait completed");
+    return rc;
+}
+
 int bs_check_device_flag(bs_sim* s) {
     if (!s->flag_armed) return BS_OK;
     s->flag_armed = false;

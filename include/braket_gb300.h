@@ -259,6 +259,11 @@ int bs_batch_set_tuning(bs_batch* batch, int n, const int* params, const double*
 
 /* synchronise the handle's stream; device pointer of the state (for in-HBM benchmarking) */
 int bs_synchronize(bs_sim* sim);
+/* Failure-detection self-test: one thread waits, with the tensor-core sweep's bounded mbarrier
+ * wait, on a barrier that nothing completes, gives up after about `seconds` (0 < seconds <= 1) of
+ * clock, and raises the handle's device flag.  Returns BS_ERR_TIMEOUT, as a sweep whose copy or MMA
+ * never landed would; the handle stays usable.  Nothing faults or hangs. */
+int bs_selftest_wait_timeout(bs_sim* sim, double seconds);
 int bs_state_device_ptr(bs_sim* sim, void** out);
 
 #ifdef __cplusplus

@@ -130,3 +130,4 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu_call():
     assert L.bs_reduced_density_matrix(None, 1, None, None) != 0
     n = C.c_int64()
     assert L.bs_write_result_file(None, 0, b"/dev/null", C.byref(n)) != 0
+    assert L.bs_selftest_wait_timeout(None, 0.01) != 0

@@ -232,3 +232,18 @@ def test_swaps_in_density_matrix_with_reference_channels():
         sim.evolve(ops)
         ref = oracle.OracleDM(n, physical=(mode == "physical")).evolve(ops).matrix
         assert rel_err(sim.density_matrix, ref) < 1e-12
+
+
+def test_bounded_wait_gives_up_and_the_handle_stays_usable():
+    """Failure detection without a fault: a wait on a barrier that nothing completes gives up after
+    its limit, the kernel raises the device flag and returns, the call reports BS_ERR_TIMEOUT, and the
+    same handle then simulates correctly."""
+    import oracle
+    sim = bs.StateVectorSimulator(8, 0)
+    with pytest.raises(bs._abi.BraketGB300Error) as e:
+        sim._h.call("bs_selftest_wait_timeout", 0.01)
+    assert e.value.code == bs._abi.BS_ERR_TIMEOUT
+    ops = random_circuit(8, 30, np.random.default_rng(41))
+    sim.evolve(ops)
+    ref = oracle.OracleSV(8).evolve(ops).psi
+    assert np.linalg.norm(sim.state_vector - ref) <= 1e-12 * np.linalg.norm(ref)
