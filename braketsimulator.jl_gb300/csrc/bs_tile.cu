@@ -276,14 +276,15 @@ __device__ void tile_kraus_ref(float4* sm, int T, int L, const TileGate& g, cons
 // kernel with fewer live registers and therefore more resident warps.
 // The reference-rule Kraus channel of tile_kraus_ref with few registers (for the tensor-core sweep,
 // whose threads have none to spare, and for the float-float sweep, whose 2-target variant would
-// otherwise need the 4-bit kernel): candidate blocks are tested 32 at a time and the ones that pass the
-// row/column test collected, then one thread per output element of a collected block sums over the
-// Kraus matrices reading the block from shared memory; all reads of the collected blocks finish
-// before any of their outputs is written.  s_act: 32 ints of shared scratch.
+// otherwise need the 4-bit kernel): candidate blocks are tested and the ones that pass the
+// row/column test collected (all candidates tested in one pass), then one thread per output element
+// of a collected block sums over the Kraus matrices reading the block from shared memory; all reads
+// of the collected blocks finish before any of their outputs is written.  s_act: 32 ints of shared
+// scratch.
 template <int K, bool SW, typename OT>
 __device__ void tile_kraus_ref_lr(float4* sm, int T, int L, const TileGate& g, const float4* __restrict__ mats,
                                   int64_t base, OT off_tab, int osh, int n, int* s_act, int* s_cnt) {
-    constexpr int D = 1 << K, DD = D * D, kChunkG = 32;   // candidate blocks per pass
+    constexpr int D = 1 << K, DD = D * D, kChunkG = 32;   // capacity of s_act: at most this many blocks pass
     const int64_t rmask = ((int64_t)1 << n) - 1;
     if ((((base & rmask) ^ (base >> n)) & (int64_t)g.pmask[1]) != 0) return;   // uniform in the CTA
     int pos[2 * K];
@@ -296,63 +297,61 @@ __device__ void tile_kraus_ref_lr(float4* sm, int T, int L, const TileGate& g, c
             if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
     const int lowmask = (1 << L) - 1, ngroups = 1 << (T - 2 * K);
     const float4* km = mats + g.mat_off;
-    for (int gs = 0; gs < ngroups; gs += kChunkG) {   // candidate blocks, one per thread of warp 0
-        if (threadIdx.x == 0) *s_cnt = 0;
-        __syncthreads();
-        if (threadIdx.x < kChunkG) {
-            const int b = gs + (int)threadIdx.x;
-            if (b < ngroups) {
-                int j0 = b;
+    // Every candidate block is tested in one pass by all threads.  A block passes when, for every
+    // non-target qubit, its row and column bits agree; each non-target tile bit belongs to a qubit
+    // whose other bit is either in the tile (one constraint per pair) or constant in the CTA (one per
+    // bit), so at most 2^((T - 2K) / 2) <= 32 blocks pass (T <= 12): s_act holds them all.
+    if (threadIdx.x == 0) *s_cnt = 0;
+    __syncthreads();
+    for (int b = (int)threadIdx.x; b < ngroups; b += (int)blockDim.x) {
+        int j0 = b;
 #pragma unroll
-                for (int q = 0; q < 2 * K; q++) j0 = insert0(j0, pos[q]);
-                const int64_t gi = base | ((int64_t)off_tab[j0 >> L] << osh) | (int64_t)(j0 & lowmask);
-                if (((((gi & rmask) ^ (gi >> n)) & (int64_t)g.pmask[0]) == 0)) s_act[atomicAdd(s_cnt, 1)] = j0;
-            }
+        for (int q = 0; q < 2 * K; q++) j0 = insert0(j0, pos[q]);
+        const int64_t gi = base | ((int64_t)off_tab[j0 >> L] << osh) | (int64_t)(j0 & lowmask);
+        if (((((gi & rmask) ^ (gi >> n)) & (int64_t)g.pmask[0]) == 0)) {
+            const int slot = atomicAdd(s_cnt, 1);
+            if (slot < kChunkG) s_act[slot] = j0;
         }
-        __syncthreads();
-        const int nact = *s_cnt;   // at most kChunkG
-        __syncthreads();           // every thread has read the count before it is reset
-        if (nact > 0) {
-            const int c0 = 0;
-            const int items = nact * DD;
-            for (int it0 = 0; it0 < items; it0 += blockDim.x) {
-                const int it = it0 + (int)threadIdx.x;
-                float4 outv = make_float4(0.f, 0.f, 0.f, 0.f);
-                int dst = -1;
-                if (it < items) {
-                    const int j0 = s_act[c0 + it / DD], e = it % DD, i = e / D, jj = e % D;
-                    auto at = [&](int r, int c) {
-                        int j = j0;
+    }
+    __syncthreads();
+    const int nact = min(*s_cnt, kChunkG);
+    const int items = nact * DD;
+    for (int it0 = 0; it0 < items; it0 += blockDim.x) {
+        const int it = it0 + (int)threadIdx.x;
+        float4 outv = make_float4(0.f, 0.f, 0.f, 0.f);
+        int dst = -1;
+        if (it < items) {
+            const int j0 = s_act[it / DD], e = it % DD, i = e / D, jj = e % D;
+            auto at = [&](int r, int c) {
+                int j = j0;
 #pragma unroll
-                        for (int q = 0; q < K; q++) {
-                            if ((r >> q) & 1) j |= 1 << g.tbit[q];
-                            if ((c >> q) & 1) j |= 1 << g.tbit[K + q];
-                        }
-                        return sx<SW>(j);
-                    };
-                    ffacc ar{0.f, 0.f}, ai{0.f, 0.f};
-                    bool first = true;
-                    for (int q = 0; q < g.npar; q++) {
-                        const float4* Kq = km + q * DD;
-                        for (int c = 0; c < D; c++) {
-                            ffacc tr, ti;
-                            cmac_first(tr, ti, f4m(__ldg(Kq + i * D)), f4c(sm[at(0, c)]));
-                            for (int r = 1; r < D; r++) cmac(tr, ti, f4m(__ldg(Kq + i * D + r)), f4c(sm[at(r, c)]));
-                            const cff t = cdone(tr, ti);
-                            const float4 kj = __ldg(Kq + jj * D + c);
-                            const cff kc = {kj.x, kj.y, -kj.z, -kj.w};
-                            if (first) { cmac_first(ar, ai, kc, t); first = false; }
-                            else cmac(ar, ai, kc, t);
-                        }
-                    }
-                    outv = c4f(cdone(ar, ai));
-                    dst = at(i, jj);
+                for (int q = 0; q < K; q++) {
+                    if ((r >> q) & 1) j |= 1 << g.tbit[q];
+                    if ((c >> q) & 1) j |= 1 << g.tbit[K + q];
                 }
-                __syncthreads();   // every read of this chunk's blocks is done
-                if (dst >= 0) sm[dst] = outv;
-                __syncthreads();
+                return sx<SW>(j);
+            };
+            ffacc ar{0.f, 0.f}, ai{0.f, 0.f};
+            bool first = true;
+            for (int q = 0; q < g.npar; q++) {
+                const float4* Kq = km + q * DD;
+                for (int c = 0; c < D; c++) {
+                    ffacc tr, ti;
+                    cmac_first(tr, ti, f4m(__ldg(Kq + i * D)), f4c(sm[at(0, c)]));
+                    for (int r = 1; r < D; r++) cmac(tr, ti, f4m(__ldg(Kq + i * D + r)), f4c(sm[at(r, c)]));
+                    const cff t = cdone(tr, ti);
+                    const float4 kj = __ldg(Kq + jj * D + c);
+                    const cff kc = {kj.x, kj.y, -kj.z, -kj.w};
+                    if (first) { cmac_first(ar, ai, kc, t); first = false; }
+                    else cmac(ar, ai, kc, t);
+                }
             }
+            outv = c4f(cdone(ar, ai));
+            dst = at(i, jj);
         }
+        __syncthreads();   // every read of the collected blocks is done
+        if (dst >= 0) sm[dst] = outv;
+        __syncthreads();
     }
 }
 
