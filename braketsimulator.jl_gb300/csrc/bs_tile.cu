@@ -207,77 +207,10 @@ __device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const flo
 // target bits; pmask[0]: row-index mask of the non-target bits; pmask[1]: the non-target bits whose
 // row and column bits both lie outside the tile (so that part of the test is uniform in the CTA);
 // npar: number of Kraus matrices, row-major D x D each at mat_off.
-template <int K, bool SW, typename OT>
-__device__ void tile_kraus_ref(float4* sm, int T, int L, const TileGate& g, const float4* __restrict__ mats,
-                               int64_t base, const OT* off_tab, int osh, int n) {
-    constexpr int D = 1 << K;
-    const int64_t rmask = ((int64_t)1 << n) - 1;
-    if ((((base & rmask) ^ (base >> n)) & (int64_t)g.pmask[1]) != 0) return;
-    int pos[2 * K];
-#pragma unroll
-    for (int q = 0; q < 2 * K; q++) pos[q] = g.tbit[q];
-#pragma unroll
-    for (int a = 0; a < 2 * K; a++)
-#pragma unroll
-        for (int b = a + 1; b < 2 * K; b++)
-            if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
-    const int lowmask = (1 << L) - 1;
-    const float4* km = mats + g.mat_off;
-    for (int b = threadIdx.x; b < (1 << (T - 2 * K)); b += blockDim.x) {
-        int j0 = b;
-#pragma unroll
-        for (int q = 0; q < 2 * K; q++) j0 = insert0(j0, pos[q]);
-        const int64_t gi = base | ((int64_t)off_tab[j0 >> L] << osh) | (int64_t)(j0 & lowmask);
-        if ((((gi & rmask) ^ (gi >> n)) & (int64_t)g.pmask[0]) != 0) continue;
-        // rho[r][c]: row target pattern r, column target pattern c
-        cff rho[D][D];
-        int idx[D][D];
-#pragma unroll
-        for (int r = 0; r < D; r++)
-#pragma unroll
-            for (int c = 0; c < D; c++) {
-                int j = j0;
-#pragma unroll
-                for (int q = 0; q < K; q++) {
-                    if ((r >> q) & 1) j |= 1 << g.tbit[q];
-                    if ((c >> q) & 1) j |= 1 << g.tbit[K + q];
-                }
-                idx[r][c] = sx<SW>(j);
-                rho[r][c] = f4c(sm[idx[r][c]]);
-            }
-        // out[i][j] = sum_q sum_c (sum_r K_q[i][r] rho[r][c]) conj(K_q[j][c]), one element at a time
-#pragma unroll 1
-        for (int i = 0; i < D; i++)
-#pragma unroll 1
-            for (int j = 0; j < D; j++) {
-                ffacc ar{0.f, 0.f}, ai{0.f, 0.f};
-                bool first = true;
-                for (int q = 0; q < g.npar; q++) {
-                    const float4* Kq = km + q * D * D;
-#pragma unroll
-                    for (int c = 0; c < D; c++) {
-                        ffacc tr, ti;
-                        cmac_first(tr, ti, f4m(__ldg(Kq + i * D)), rho[0][c]);
-#pragma unroll
-                        for (int r = 1; r < D; r++) cmac(tr, ti, f4m(__ldg(Kq + i * D + r)), rho[r][c]);
-                        const cff t = cdone(tr, ti);
-                        const float4 kj = __ldg(Kq + j * D + c);
-                        const cff kc = {kj.x, kj.y, -kj.z, -kj.w};
-                        if (first) { cmac_first(ar, ai, kc, t); first = false; }
-                        else cmac(ar, ai, kc, t);
-                    }
-                }
-                sm[idx[i][j]] = c4f(cdone(ar, ai));
-            }
-    }
-}
-
-// KMAX: widest dense/monomial gate of the sweep (2 or 4); narrow sweeps get a
-// kernel with fewer live registers and therefore more resident warps.
-// The reference-rule Kraus channel of tile_kraus_ref with few registers (for the tensor-core sweep,
-// whose threads have none to spare, and for the float-float sweep, whose 2-target variant would
-// otherwise need the 4-bit kernel): candidate blocks are tested and the ones that pass the
-// row/column test collected (all candidates tested in one pass), then one thread per output element
+// With few registers (the tensor-core sweep's threads have none to spare, and the float-float
+// sweep's 2-target variant would otherwise need the 4-bit kernel): candidate blocks are tested and
+// the ones that pass the row/column test collected (all candidates tested in one pass), then one
+// thread per output element
 // of a collected block sums over the Kraus matrices reading the block from shared memory; all reads
 // of the collected blocks finish before any of their outputs is written.  s_act: 32 ints of shared
 // scratch.
@@ -355,6 +288,8 @@ __device__ void tile_kraus_ref_lr(float4* sm, int T, int L, const TileGate& g, c
     }
 }
 
+// KMAX: widest dense/monomial gate of the sweep (2 or 4); narrow sweeps get a
+// kernel with fewer live registers and therefore more resident warps.
 template <int KMAX, int NT>
 __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, SweepDesc d, int64_t tile0) {
     extern __shared__ float4 smem[];
