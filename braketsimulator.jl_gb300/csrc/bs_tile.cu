@@ -313,9 +313,20 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
     __syncthreads();
     const int64_t base = s_base;
     const int lowmask = (1 << L) - 1;
-    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
-        int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
-        smem[j] = c4f(load_c128(__ldcs(psi + gidx)));
+    // tile load: eight loads per thread in flight at a time (tiles are at most 2^12 amplitudes)
+#pragma unroll
+    for (int r = 0; r < 4096 / NT; r += 8) {
+        double2 x[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int j = (r + i) * NT + (int)threadIdx.x;
+            if (j < nt) x[i] = __ldcs(psi + (base | off_tab[j >> L] | (int64_t)(j & lowmask)));
+        }
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int j = (r + i) * NT + (int)threadIdx.x;
+            if (j < nt) smem[j] = c4f(load_c128(x[i]));
+        }
     }
     __syncthreads();
     __shared__ TileGate s_gates[kGateChunk];
@@ -791,8 +802,21 @@ __global__ void __launch_bounds__(kThreads, KMAX == 2 ? 4 : 3) k_tile_sweep_c64(
     __syncthreads();
     const int64_t base = s_base;
     const int lowmask = (1 << L) - 1;
-    for (int j = threadIdx.x; j < nt; j += blockDim.x)
-        smem[j] = __ldcs(psi + (base | off_tab[j >> L] | (int64_t)(j & lowmask)));
+    // tile load: eight loads per thread in flight at a time (tiles are at most 2^12 amplitudes)
+#pragma unroll
+    for (int r = 0; r < 4096 / kThreads; r += 8) {
+        float2 x[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int j = (r + i) * kThreads + (int)threadIdx.x;
+            if (j < nt) x[i] = __ldcs(psi + (base | off_tab[j >> L] | (int64_t)(j & lowmask)));
+        }
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int j = (r + i) * kThreads + (int)threadIdx.x;
+            if (j < nt) smem[j] = x[i];
+        }
+    }
     __syncthreads();
     __shared__ TileGate s_gates[kGateChunk];
     for (int g0 = 0; g0 < d.n_gates; g0 += kGateChunk) {
