@@ -223,10 +223,27 @@ __global__ void __launch_bounds__(kAThreads) k_adjoint_sweep(typename Elem<C64>:
     __syncthreads();
     const int64_t base = s_base;
     const int lowmask = (1 << L) - 1;
-    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
-        int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
-        sp[j] = c4f(Elem<C64>::load(psi[gidx]));
-        sl[j] = c4f(Elem<C64>::load(lam[gidx]));
+    // tile loads: four positions (eight loads) per thread in flight at a time (tiles <= 2^12)
+#pragma unroll
+    for (int r = 0; r < 4096 / kAThreads; r += 4) {
+        typename Elem<C64>::T xp[4], xl[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int j = (r + i) * kAThreads + (int)threadIdx.x;
+            if (j < nt) {
+                const int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+                xp[i] = psi[gidx];
+                xl[i] = lam[gidx];
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int j = (r + i) * kAThreads + (int)threadIdx.x;
+            if (j < nt) {
+                sp[j] = c4f(Elem<C64>::load(xp[i]));
+                sl[j] = c4f(Elem<C64>::load(xl[i]));
+            }
+        }
     }
     __syncthreads();
     for (int gi = 0; gi < d.n_gates; gi++) {
