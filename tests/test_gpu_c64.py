@@ -77,3 +77,24 @@ def test_c64_state_roundtrip_and_copy():
     assert np.allclose(s.state_vector, v.astype(np.complex64), rtol=0, atol=0)
     c = s.copy()
     assert np.array_equal(c.state_vector, s.state_vector)
+
+
+def test_c64_runs_on_qubit_pairs_fold_into_two_bit_gates():
+    """Complex64 sweeps fold runs of 1- and 2-qubit gates on the same two qubits (controls in the
+    tile, or out of it) into dense 2-bit gates: same result as the oracle within FP32 error."""
+    n = 16
+    rng = np.random.default_rng(77)
+    ops = []
+    for _ in range(12):
+        a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+        c = int(rng.integers(n))
+        for ix in (bs.Instruction(bs.H(), [a]), bs.Instruction(bs.CNot(), [a, b]),
+                   bs.Instruction(bs.Rz(float(rng.uniform(-3, 3))), [b]), bs.Instruction(bs.CZ(), [b, a]),
+                   bs.Instruction(bs.Ry(float(rng.uniform(-3, 3))), [a]), bs.Instruction(bs.Swap(), [a, b]),
+                   bs.Instruction(bs.Rx(float(rng.uniform(-3, 3))), [c])):
+            ops.append(ix)
+        if c not in (a, b):
+            ops.append(bs.Instruction(bs.CCNot(), [c, a, b]))
+    sim = bs.StateVectorSimulator(n, 0, precision="c64").evolve(ops)
+    err = rel_err(sim.state_vector, oracle.OracleSV(n).evolve(ops).psi)
+    assert err < 2e-5, err
