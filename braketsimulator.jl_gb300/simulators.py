@@ -12,12 +12,13 @@ from __future__ import annotations
 import ctypes as C
 import math
 import os
+import struct
 from typing import Sequence
 
 import numpy as np
 
 from . import _abi
-from .gates import Barrier, Control, Delay, Gate, Measure, Reset, Unitary, lower_gate
+from .gates import Barrier, Control, Delay, Gate, Measure, Reset, Rx, Ry, Rz, Unitary, lower_gate
 from .noises import Noise, lower_noise
 from .observables import (H, HermitianObservable, I, Observable, StandardObservable, TensorProduct, X, Y, Z,
                           diagonalizing_gates)
@@ -84,8 +85,27 @@ _LOWER_CACHE: dict = {}
 _LOWER_CACHE_MAX = 1 << 16
 
 
+_BSOP_SIZE = C.sizeof(_abi.BsOp)
+_OFF_NT, _OFF_T0, _OFF_MAT = _abi.BsOp.n_targets.offset, _abi.BsOp.targets.offset, _abi.BsOp.matrix.offset
+_ROTATIONS = (Rx, Ry, Rz)
+
+
+def _rotation_op(op, q: int):
+    """The lowering of a 1-qubit rotation (what lower_gate gives: its dense matrix_rep, no flags),
+    without the generic dispatch: rotations in variational and random circuits rarely repeat an
+    angle, so they miss the cache and their lowering cost is the batch's host time."""
+    buf = _abi.cplx_buffer(op.matrix_rep())
+    b = bytearray(_BSOP_SIZE)
+    struct.pack_into("<i", b, _OFF_NT, 1)
+    struct.pack_into("<i", b, _OFF_T0, q)
+    struct.pack_into("<Q", b, _OFF_MAT, buf.ctypes.data)
+    return [(bytes(b), buf)]
+
+
 def _gate_ops(op, t):
     """[(bs_op struct bytes, matrix buffer)] for one gate on targets t (a tuple of ints)."""
+    if type(op) in _ROTATIONS and len(t) == 1:
+        return _rotation_op(op, t[0])
     key = None
     if not isinstance(op, (Unitary, Control)):
         key = (type(op), op.angle, op.pow_exponent, t)

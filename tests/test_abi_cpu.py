@@ -131,3 +131,21 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu_call():
     n = C.c_int64()
     assert L.bs_write_result_file(None, 0, b"/dev/null", C.byref(n)) != 0
     assert L.bs_selftest_wait_timeout(None, 0.01) != 0
+
+
+def test_rotation_fast_lowering_matches_generic_lowering():
+    """1-qubit rotations skip the generic dispatch; the op struct and matrix they produce are the
+    generic lowering's (no flags, one target, the gate's own matrix_rep, powers included)."""
+    import numpy as np
+    from braketsimulator_gb300 import gates as G, simulators as S
+    rng = np.random.default_rng(1)
+    for cls in (G.Rx, G.Ry, G.Rz):
+        for pw in (1.0, 0.5, -2.0):
+            g = cls(float(rng.uniform(-7, 7)), pow_exponent=pw)
+            q = int(rng.integers(20))
+            (raw, buf), = S._rotation_op(g, q)
+            (lg,) = G.lower_gate(g, (q,))
+            o = bs._abi.BsOp.from_buffer_copy(raw)
+            assert (o.kind, o.flags, o.n_targets, o.targets[0], o.n_controls, o.n_matrices) == (0, lg.flags, 1, q, 0, 0)
+            assert np.array_equal(buf, bs._abi.cplx_buffer(lg.matrix))
+            assert S._gate_ops(g, (q,))[0][1].dtype == np.float64
