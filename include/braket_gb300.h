@@ -259,7 +259,7 @@ int bs_batch_set_tuning(bs_batch* batch, int n, const int* params, const double*
 
 /* synchronise the handle's stream; device pointer of the state (for in-HBM benchmarking) */
 int bs_synchronize(bs_sim* sim);
-/* Failure-detection self-test: one thread waits, with the tensor-core sweep's bounded mbarrier
+/* Failure-detection self-test (no reference counterpart): one thread waits, with the tensor-core sweep's bounded mbarrier
  * wait, on a barrier that nothing completes, gives up after about `seconds` (0 < seconds <= 1) of
  * clock, and raises the handle's device flag.  Returns BS_ERR_TIMEOUT, as a sweep whose copy or MMA
  * never landed would; the handle stays usable.  Nothing faults or hangs. */
