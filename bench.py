@@ -184,7 +184,9 @@ def cpu_baseline_port(seconds_budget=20.0):
                       f"{dt:.1f} s on {cores} OpenMP threads"}, dt
 
 
-def adjoint_bench(bs, n=24, layers=10, terms=48, shift_params=24, seed=3):
+def adjoint_bench(bs, n=24, layers=10, terms=48, shift_params=24, seed=3, ansatz="ry_rz_zz", c64=True):
+    """ansatz "ry_rz_zz": per layer Ry(t) Rz(t) on every qubit and a ZZ(t) ring (720 parameters at 24
+    qubits, 10 layers); "ry_cz": per layer Ry(t) on every qubit and a fixed CZ ring (240 parameters)."""
     from importlib import import_module
     adj = import_module("braketsimulator_gb300.adjoint")
     rng = np.random.default_rng(seed)
@@ -192,9 +194,13 @@ def adjoint_bench(bs, n=24, layers=10, terms=48, shift_params=24, seed=3):
     for _ in range(layers):
         for q in range(n):
             ops.append(bs.Instruction(bs.Ry(float(rng.uniform(-np.pi, np.pi))), [q]))
-            ops.append(bs.Instruction(bs.Rz(float(rng.uniform(-np.pi, np.pi))), [q]))
+            if ansatz == "ry_rz_zz":
+                ops.append(bs.Instruction(bs.Rz(float(rng.uniform(-np.pi, np.pi))), [q]))
         for q in range(n):
-            ops.append(bs.Instruction(bs.ZZ(float(rng.uniform(-np.pi, np.pi))), [q, (q + 1) % n]))
+            if ansatz == "ry_rz_zz":
+                ops.append(bs.Instruction(bs.ZZ(float(rng.uniform(-np.pi, np.pi))), [q, (q + 1) % n]))
+            else:
+                ops.append(bs.Instruction(bs.CZ(), [q, (q + 1) % n]))
     h = []
     for _ in range(terms):
         w = int(rng.integers(1, 5))
@@ -226,6 +232,15 @@ def adjoint_bench(bs, n=24, layers=10, terms=48, shift_params=24, seed=3):
     torch.cuda.synchronize()
     t_ps_per_param = (time.perf_counter() - t0) / shift_params
     P = len(pidx)
+    base = {"qubits": n, "params": P, "terms": terms, "energy": e,
+            "adjoint_s_per_gradient": round(t_adj, 4), "adjoint_grads_per_s": round(P / t_adj, 1),
+            "param_shift_s_per_gradient_extrapolated": round(t_ps_per_param * P, 3),
+            "param_shift_grads_per_s": round(1.0 / t_ps_per_param, 2),
+            "speedup_vs_param_shift": round(t_ps_per_param * P / t_adj, 1),
+            "max_abs_diff_vs_param_shift": float(max(diffs)),
+            "param_shift_sample": f"{shift_params} of {P} parameters, 2 circuits each"}
+    if not c64:
+        return base
     # complex64 variant: same circuit and Hamiltonian on a complex64 state
     sim64 = bs.StateVectorSimulator(n, 0, precision="c64")
     adj.adjoint_gradient(sim64, ops, h)
@@ -235,16 +250,10 @@ def adjoint_bench(bs, n=24, layers=10, terms=48, shift_params=24, seed=3):
         e64, g64 = adj.adjoint_gradient(sim64, ops, h)
     torch.cuda.synchronize()
     t_adj64 = (time.perf_counter() - t0) / reps
-    return {"qubits": n, "params": P, "terms": terms, "energy": e,
+    return {**base,
             "c64": {"adjoint_s_per_gradient": round(t_adj64, 4), "adjoint_grads_per_s": round(P / t_adj64, 1),
                     "max_abs_diff_vs_c128_gradient": float(np.max(np.abs(np.asarray(g64) - np.asarray(g)))),
-                    "energy_diff_vs_c128": float(abs(e64 - e))},
-            "adjoint_s_per_gradient": round(t_adj, 4), "adjoint_grads_per_s": round(P / t_adj, 1),
-            "param_shift_s_per_gradient_extrapolated": round(t_ps_per_param * P, 3),
-            "param_shift_grads_per_s": round(1.0 / t_ps_per_param, 2),
-            "speedup_vs_param_shift": round(t_ps_per_param * P / t_adj, 1),
-            "max_abs_diff_vs_param_shift": float(max(diffs)),
-            "param_shift_sample": f"{shift_params} of {P} parameters, 2 circuits each"}
+                    "energy_diff_vs_c128": float(abs(e64 - e))}}
 
 
 def ghz_bench(bs, reps=100, cpu=False):
@@ -599,6 +608,7 @@ def main():
         line["cpu_baseline"], _ = cpu_baseline_port()
     if not args.no_adjoint:
         line["adjoint"] = adjoint_bench(bs)
+        line["adjoint240"] = adjoint_bench(bs, ansatz="ry_cz", c64=False)   # the 240-parameter ansatz
         line["ghz10"] = ghz_bench(bs, cpu=not args.no_cpu)
         line["dm14"] = dm_bench(bs, cpu=not args.no_cpu)
         line["batch512"] = batch_bench(bs, cpu=not args.no_cpu)
