@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(kAThreads) k_adjoint_sweep(typename Elem<C64>:
     }
     __syncthreads();
     for (int gi = 0; gi < d.n_gates; gi++) {
-        const AdjGate a = ag[gi];
+        const AdjGate& a = ag[gi];   // fields read where used (a copy of the whole descriptor went to local memory)
         if (a.g.kind == 3) {
             // Im <lambda| G |psi> over the tile
             ffsum acc{0.f, 0.f};
