@@ -469,17 +469,17 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const TileG
         return;
     }
     const f2 osc2 = pk(osc, osc);
-    uint32_t eb = 0;
+    float mx = 0.f;   // largest |high word|: its exponent field is the largest exponent field
 #pragma unroll
     for (int a = 0; a < NA; a++) {
         const f2 hs = add2(S[a], E[a]);
         const f2 ls = sub2(E[a], sub2(hs, S[a]));
         const float2 hh = up(mul2(hs, osc2)), ll = up(mul2(ls, osc2));
         sm[spm ^ tsw[a]] = make_float4(hh.x, hh.y, ll.x, ll.y);
-        eb = max(eb, max(__float_as_uint(hh.x) & 0x7F800000u, __float_as_uint(hh.y) & 0x7F800000u));
+        mx = fmaxf(mx, fmaxf(fabsf(hh.x), fabsf(hh.y)));
     }
     // the next fused gate's tile scale (read after the caller's barrier)
-    eb = __reduce_max_sync(0xffffffffu, eb);
+    const uint32_t eb = __reduce_max_sync(0xffffffffu, __float_as_uint(mx) & 0x7F800000u);
     if (lane_id == 0) s_wmax[warp] = eb;
 }
 
