@@ -195,6 +195,75 @@ __device__ void adj_apply(float4* sm, int T, int L, const TileGate& g, const flo
     }
 }
 
+// The same gate on both tiles of the sweep (psi and lambda) in one pass: the index arithmetic and the
+// matrix reads are shared.  Dense gates on 1 or 2 targets and diagonal gates; others go through
+// adj_apply once per tile.
+template <int K>
+__device__ void adj_dense2(float4* sa, float4* sb, int T, const TileGate& g, const float4* __restrict__ mats) {
+    constexpr int D = 1 << K;
+    int pos[K];
+    for (int q = 0; q < K; q++) pos[q] = g.tbit[q];
+    for (int a = 0; a < K; a++)
+        for (int b = a + 1; b < K; b++)
+            if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
+    const int ngroups = 1 << (T - K);
+    const float4* m = mats + g.mat_off;
+    for (int gr = threadIdx.x; gr < ngroups; gr += blockDim.x) {
+        int jb = gr;
+        for (int q = 0; q < K; q++) { int low = jb & ((1 << pos[q]) - 1); jb = ((jb >> pos[q]) << (pos[q] + 1)) | low; }
+        if ((jb & (int)g.lc_mask) != (int)g.lc_val) continue;
+        cff x[D], y[D];
+        int idx[D];
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+            int j = jb;
+            for (int q = 0; q < K; q++) if ((c >> q) & 1) j |= 1 << g.tbit[q];
+            idx[c] = j;
+            x[c] = f4c(sa[j]);
+            y[c] = f4c(sb[j]);
+        }
+#pragma unroll
+        for (int r = 0; r < D; r++) {
+            ffacc ar, ai, br, bi;
+            const cff m0 = f4c(__ldg(m + r * D));
+            cmac_first(ar, ai, m0, x[0]);
+            cmac_first(br, bi, m0, y[0]);
+#pragma unroll
+            for (int c = 1; c < D; c++) {
+                const cff mc = f4c(__ldg(m + r * D + c));
+                cmac(ar, ai, mc, x[c]);
+                cmac(br, bi, mc, y[c]);
+            }
+            sa[idx[r]] = c4f(cdone(ar, ai));
+            sb[idx[r]] = c4f(cdone(br, bi));
+        }
+    }
+}
+
+__device__ void adj_apply2(float4* sa, float4* sb, int T, int L, const TileGate& g, const float4* mats,
+                           const int32_t* perms, int64_t base, const int64_t* off_tab) {
+    if (g.kind == 1) {
+        const int nt = 1 << T, lowmask = (1 << L) - 1;
+        const float4* m = mats + g.mat_off;
+        for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+            if ((j & (int)g.lc_mask) != (int)g.lc_val) continue;
+            const int64_t gi = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+            int di = 0;
+            for (int q = 0; q < g.k; q++) di |= (int)((gi >> g.gbit[q]) & 1) << q;
+            const cff dv = f4c(__ldg(m + di));
+            sa[j] = c4f(cmul(dv, f4c(sa[j])));
+            sb[j] = c4f(cmul(dv, f4c(sb[j])));
+        }
+    } else if (g.kind == 0 && g.k == 1) {
+        adj_dense2<1>(sa, sb, T, g, mats);
+    } else if (g.kind == 0 && g.k == 2) {
+        adj_dense2<2>(sa, sb, T, g, mats);
+    } else {
+        adj_apply(sa, T, L, g, mats, perms, base, off_tab);
+        adj_apply(sb, T, L, g, mats, perms, base, off_tab);
+    }
+}
+
 template <bool C64>
 __global__ void __launch_bounds__(kAThreads) k_adjoint_sweep(typename Elem<C64>::T* __restrict__ psi,
                                                              typename Elem<C64>::T* __restrict__ lam, SweepDesc d,
@@ -284,8 +353,7 @@ __global__ void __launch_bounds__(kAThreads) k_adjoint_sweep(typename Elem<C64>:
             continue;
         }
         if ((base & (int64_t)a.g.gc_mask) != (int64_t)a.g.gc_val) continue;
-        adj_apply(sp, T, L, a.g, d.mats, d.perms, base, off_tab);
-        adj_apply(sl, T, L, a.g, d.mats, d.perms, base, off_tab);
+        adj_apply2(sp, sl, T, L, a.g, d.mats, d.perms, base, off_tab);
         __syncthreads();
     }
     for (int j = threadIdx.x; j < nt; j += blockDim.x) {
