@@ -52,15 +52,20 @@ def haar_su2(rng):
     return q / np.sqrt(np.linalg.det(q))
 
 
-def dense_circuit(bs, n=N_QUBITS, layers=LAYERS, seed=0):
+def dense_circuit(bs, n=N_QUBITS, layers=LAYERS, seed=0, layers2=None, two_qubit="cz"):
+    """The dense random circuit: `layers` layers of Haar SU(2) on every qubit and a 2-qubit gate on
+    an alternating even/odd brick, then `layers2` (default `layers`) layers of SU(2) on every qubit
+    and the 2-qubit gate at (q, q+s mod n), s cycling through 1, 8, 16.  two_qubit: "cz" (the
+    headline workload) or "cnot" (a dense 2-qubit gate that fusion cannot fold into a phase)."""
     rng = np.random.default_rng(seed)
+    gate = {"cz": bs.CZ, "cnot": bs.CNot}[two_qubit]
     ops = []
     for layer in range(layers):
         for q in range(n):
             ops.append(bs.Instruction(bs.Unitary(haar_su2(rng)), [q]))
         for q in range(layer % 2, n - 1, 2):
-            ops.append(bs.Instruction(bs.CZ(), [q, q + 1]))
-    for layer in range(layers):
+            ops.append(bs.Instruction(gate(), [q, q + 1]))
+    for layer in range(layers if layers2 is None else layers2):
         s = STRIDES[layer % len(STRIDES)]
         for q in range(n):
             ops.append(bs.Instruction(bs.Unitary(haar_su2(rng)), [q]))
@@ -70,8 +75,20 @@ def dense_circuit(bs, n=N_QUBITS, layers=LAYERS, seed=0):
             if q in used or r in used:
                 continue
             used.update((q, r))
-            ops.append(bs.Instruction(bs.CZ(), [q, r]))
+            ops.append(bs.Instruction(gate(), [q, r]))
     return ops
+
+
+def inverse_circuit(bs, ops):
+    """The circuit's inverse: reversed order, each SU(2) daggered (CZ and CNOT are involutions)."""
+    out = []
+    for ix in reversed(ops):
+        g = ix.operator
+        if isinstance(g, bs.Unitary):
+            out.append(bs.Instruction(bs.Unitary(np.conj(np.asarray(g.matrix)).T), list(ix.target)))
+        else:
+            out.append(bs.Instruction(type(g)(), list(ix.target)))
+    return out
 
 
 class Clocks:
@@ -155,40 +172,152 @@ def step(bs, sim, ops, shots, seed):
     return st, e, s
 
 
-def cpu_baseline_port(seconds_budget=20.0):
-    """The oracle (C restatement of the reference's kernels, OpenMP over host cores) on a
-    bounded sample of the workload: SU(2) sweeps and CZ sweeps of the 30-qubit state."""
-    import oracle
-    L = oracle.lib()
-    n = N_QUBITS
-    psi = np.zeros(2 ** n, dtype=np.complex128)
-    psi[0] = 1.0
-    rng = np.random.default_rng(1)
-    cores = os.cpu_count() or 1
+class ReferenceSampler:
+    """The reference's CPU path for the headline workload, on the oracle port of its kernels
+    (Julia is not installed: C restatements of src/gate_kernels.jl, OpenMP over the host cores
+    as the reference's Threads.@threads), timed on bounded samples and extrapolated to a step.
+
+    One step of the workload on the reference path is
+      evolve!:       each of the circuit's instructions through the reference's dispatch (SU(2)
+                     as a 1-qubit dense sweep, CZ as the 1-control-1-target kernel that touches
+                     half of the amplitudes, src/gate_kernels.jl:489-537,579-606,720-732);
+      expectation:   <Z0 Z29> = real(dot(psi, apply_observable(Z Z, copy(psi)))), a deep copy, two
+                     Z sweeps and a dot (src/sv_simulator.jl:240-248);
+      probabilities: abs2 of the state and the pairwise sum of Weights (src/result_types.jl:56-58);
+      1e5 shots:     at 30 qubits the reference draws every shot by StatsBase's linear scan of the
+                     running sum (src/result_types.jl:73-77), about 2^29 weights per shot for the
+                     circuit's flat (Porter-Thomas) output distribution.
+    Each sample evolves the next contiguous slice of the instruction list on a persistent 30-qubit
+    oracle state (so over the steps the oracle runs the circuit from its start), and times one of
+    the other three parts in rotation; the step estimate is n_SU(2) * t_SU(2) + n_CZ * t_CZ +
+    t_expectation + t_probabilities + 1e5 * t_shot from the running means."""
+
+    def __init__(self, bs, ops):
+        import oracle
+        self.oracle = oracle
+        oracle.lib()
+        self.ops = ops
+        self.unitary = bs.Unitary
+        self.n_su2 = sum(1 for ix in ops if isinstance(ix.operator, bs.Unitary))
+        self.n_2q = len(ops) - self.n_su2
+        self.sv = oracle.OracleSV(N_QUBITS)
+        self.cursor = 0
+        self.t = {"su2": [], "2q": [], "expectation": [], "probabilities": [], "shot": []}
+        self.flat = None
+        self.part = 0
+        self.cores = os.cpu_count() or 1
+
+    def _time(self, key, fn):
+        t0 = time.perf_counter()
+        r = fn()
+        self.t[key].append(time.perf_counter() - t0)
+        return r
+
+    def expectation(self):
+        zz = (1 << 0) | (1 << (N_QUBITS - 1))
+        self._time("expectation", lambda: self.oracle.expectation_pauli_sv(self.sv.psi, N_QUBITS, 0, zz))
+
+    def probabilities(self):
+        self._time("probabilities", lambda: self.oracle.pairwise_sum(np.abs(self.sv.psi) ** 2))
+
+    def shot(self):
+        if N_QUBITS >= 30:
+            # one draw at u = 1/2 on a flat weight vector: the scan covers half of the 2^n weights,
+            # the mean over uniform draws for a flat cumulative distribution
+            if self.flat is None:
+                self.flat = np.full(2 ** N_QUBITS, 2.0 ** -N_QUBITS)
+            self._time("shot", lambda: self.oracle.sample_direct(self.flat, np.array([0.5]), 1.0))
+        else:
+            # below 30 qubits the reference builds the alias table and draws from it
+            # (src/result_types.jl:62-72): its cost per step, spread over the shots
+            p = np.abs(self.sv.psi) ** 2
+            rng = np.random.default_rng(0)
+
+            def draw():
+                ap, al = self.oracle.alias_table(p)
+                self.oracle.sample_alias(ap, al, rng.integers(0, p.size, SHOTS), rng.random(SHOTS))
+
+            t0 = time.perf_counter()
+            draw()
+            self.t["shot"].append((time.perf_counter() - t0) / SHOTS)
+
+    def sample(self, n_gates=8, parts=None):
+        """Evolve the next n_gates instructions; time the parts named (default: the next in rotation)."""
+        for _ in range(n_gates):
+            ix = self.ops[self.cursor]
+            self._time("su2" if isinstance(ix.operator, self.unitary) else "2q", lambda: self.sv.evolve([ix]))
+            self.cursor = (self.cursor + 1) % len(self.ops)
+            if self.cursor == 0:
+                self.sv = self.oracle.OracleSV(N_QUBITS)
+        rot = ("expectation", "probabilities", "shot")
+        if parts is None:
+            parts = [rot[self.part % 3]]
+            self.part += 1
+        for p in parts:
+            getattr(self, p)()
+
+    def estimate(self):
+        """Seconds per step of the whole workload on the reference path, and its parts."""
+        m = {k: (float(np.mean(v)) if v else float("nan")) for k, v in self.t.items()}
+        parts = {"evolve": self.n_su2 * m["su2"] + self.n_2q * m["2q"], "expectation": m["expectation"],
+                 "probabilities": m["probabilities"], "shots": SHOTS * m["shot"]}
+        return sum(parts.values()), parts
+
+    def describe(self):
+        c = {k: len(v) for k, v in self.t.items()}
+        return (f"oracle port of the reference kernels on {self.cores} OpenMP threads: {c['su2']} SU(2) and {c['2q']} "
+                f"CZ instructions of the workload timed one by one through the reference dispatch, "
+                f"{c['expectation']} <Z0 Z{N_QUBITS - 1}> evaluations, {c['probabilities']} probability passes and "
+                f"{c['shot']} " + (f"direct-sampling scans (2^{N_QUBITS - 1} weights each)" if N_QUBITS >= 30 else
+                                   f"alias-table builds with {SHOTS} draws") +
+                f" of the {N_QUBITS}-qubit state; the step "
+                f"({self.n_su2} SU(2) + {self.n_2q} CZ, <Z0 Z{N_QUBITS - 1}>, probabilities, {SHOTS} shots) "
+                f"extrapolated from "
+                f"their means")
+
+
+def headline_check(bs, sim, ops, zz):
+    """Checks of the benchmarked 30-qubit result itself, after the timed region (the FP64 oracle
+    runs this circuit in the test suite at 28 qubits and a shortened one at 30; at full size it
+    would take minutes of host time):
+      mirror: the inverse circuit applied to the benchmarked state must give back |0...0>;
+      paths:  <Z0 Z29> from the tensor-core sweeps against the float-float sweeps alone (BS_TC off),
+              two independent arithmetic paths of the engine on the same circuit."""
+    sim.evolve(inverse_circuit(bs, ops))
+    psi = sim.state_vector
+    mirror = float(np.sqrt(abs(psi[0] - 1.0) ** 2 + np.vdot(psi[1:], psi[1:]).real))
+    del psi
+    ff = bs.StateVectorSimulator(N_QUBITS, 0)
+    bs.set_tuning(ff, tc=0)
+    ff.evolve(ops)
+    zz_ff = ff.expectation(bs.observables.TensorProduct([bs.observables.Z(), bs.observables.Z()]), 0, N_QUBITS - 1)
+    del ff
+    return {"zz": zz, "zz_float_float_path": zz_ff, "zz_abs_diff": abs(zz - zz_ff),
+            "mirror_err": mirror, "tol": 1e-12, "checked": bool(mirror < 1e-12 and abs(zz - zz_ff) < 1e-12)}
+
+
+def cpu_baseline_reference(bs, ops, budget_s=25.0):
+    """cpu_baseline for the headline line: a bounded sample (about budget_s of host work)."""
+    rs = ReferenceSampler(bs, ops)
+    rs.sample(n_gates=4, parts=("expectation", "probabilities", "shot"))
     t0 = time.perf_counter()
-    sweeps = 0
-    q = 0
-    while time.perf_counter() - t0 < seconds_budget and sweeps < 64:
-        u = np.ascontiguousarray(haar_su2(rng))
-        L.orc_apply_1q(psi.ctypes.data, psi.size, u.ctypes.data, q)
-        sweeps += 1
-        if sweeps % 3 == 0:
-            cz = np.ascontiguousarray(np.diag([1, 1, 1, -1]).astype(np.complex128))
-            L.orc_apply_2q(psi.ctypes.data, psi.size, cz.ctypes.data, q, (q + 1) % n)
-            sweeps += 1
-        q = (q + 7) % n
-    dt = time.perf_counter() - t0
-    gbs = sweeps * 32.0 * 2 ** n / dt / 1e9
-    return {"value": round(gbs, 2), "unit": "GB/s", "cores": cores, "kind": "port",
-            "sample": f"{sweeps} reference-kernel gate sweeps (SU(2) and CZ) of the 30-qubit complex128 state, "
-                      f"{dt:.1f} s on {cores} OpenMP threads"}, dt
+    while time.perf_counter() - t0 < budget_s * 0.5:
+        rs.sample(n_gates=4, parts=())
+    t_step, parts = rs.estimate()
+    workload_bytes = len(ops) * 32.0 * 2 ** N_QUBITS
+    out = {"value": round(workload_bytes / t_step / 1e9, 3), "unit": "GB/s", "cores": rs.cores, "kind": "port",
+           "sample": rs.describe(),
+           "extrapolated_s_per_step": round(t_step, 1), "parts_s": {k: round(v, 2) for k, v in parts.items()},
+           "evolve_only_GBps": round(workload_bytes / parts["evolve"] / 1e9, 2)}
+    del rs
+    return out
 
 
-def adjoint_bench(bs, n=24, layers=10, terms=48, shift_params=24, seed=3, ansatz="ry_rz_zz", c64=True):
-    """ansatz "ry_rz_zz": per layer Ry(t) Rz(t) on every qubit and a ZZ(t) ring (720 parameters at 24
-    qubits, 10 layers); "ry_cz": per layer Ry(t) on every qubit and a fixed CZ ring (240 parameters)."""
-    from importlib import import_module
-    adj = import_module("braketsimulator_gb300.adjoint")
+def adjoint_workload(bs, n=24, layers=10, terms=48, seed=3, ansatz="ry_rz_zz"):
+    """(instructions, hamiltonian) of the adjoint-gradient workload.  ansatz "ry_rz_zz": per layer
+    Ry(t) Rz(t) on every qubit and a ZZ(t) ring (720 parameters at 24 qubits, 10 layers); "ry_cz":
+    per layer Ry(t) on every qubit and a fixed CZ ring (240 parameters).  Angles U(-pi, pi); the
+    Hamiltonian has `terms` Pauli strings of weight <= 4 with N(0, 1) coefficients."""
     rng = np.random.default_rng(seed)
     ops = []
     for _ in range(layers):
@@ -206,6 +335,16 @@ def adjoint_bench(bs, n=24, layers=10, terms=48, shift_params=24, seed=3, ansatz
         w = int(rng.integers(1, 5))
         qs = rng.choice(n, w, replace=False)
         h.append((float(rng.normal()), {int(q): "XYZ"[rng.integers(3)] for q in qs}))
+    return ops, h
+
+
+def adjoint_bench(bs, n=24, layers=10, terms=48, shift_params=24, seed=3, ansatz="ry_rz_zz", c64=True):
+    """ansatz "ry_rz_zz": per layer Ry(t) Rz(t) on every qubit and a ZZ(t) ring (720 parameters at 24
+    qubits, 10 layers); "ry_cz": per layer Ry(t) on every qubit and a fixed CZ ring (240 parameters)."""
+    from importlib import import_module
+    adj = import_module("braketsimulator_gb300.adjoint")
+    ops, h = adjoint_workload(bs, n, layers, terms, seed, ansatz)
+    rng = np.random.default_rng(seed + 1)
     sim = bs.StateVectorSimulator(n, 0)
     adj.adjoint_gradient(sim, ops, h)            # warm-up
     import torch
@@ -477,30 +616,75 @@ def max_over_ranks(vals, world, device="cuda"):
     return [float(x) for x in t]
 
 
+class OracleCircuit:
+    """Circuit objects for the reference arm, read by the oracle by attribute (name, angle,
+    pow_exponent, matrix): the reference arm never imports the engine."""
+
+    class Instruction:
+        def __init__(self, operator, target):
+            self.operator, self.target = operator, list(target)
+
+    class Unitary:
+        name = "unitary"
+        angle = ()
+        pow_exponent = 1.0
+
+        def __init__(self, matrix):
+            self.matrix = np.asarray(matrix, dtype=np.complex128)
+
+    class CZ:
+        name = "cz"
+        angle = ()
+        pow_exponent = 1.0
+
+    class CNot:
+        name = "cnot"
+        angle = ()
+        pow_exponent = 1.0
+
+
+def workload_config(world, n_gates):
+    """The config both arms report (identical dicts: same circuit, same outputs, same bytes)."""
+    return {"workload": workload_name(), "qubits": N_QUBITS, "gates": n_gates, "shots": SHOTS,
+            "outputs": f"<Z0 Z{N_QUBITS - 1}> and {SHOTS} shots",
+            "bytes": "gate-layer bytes: 2*16*2^n per gate (one pass per gate, as the reference runs)",
+            "l2": l2_note(), "parallelism": "replicas" if world > 1 else "1 GPU"}
+
+
 def run_reference(args, rank, world):
-    """--impl reference: the reference's CPU kernels (oracle port; Julia is not installed)
-    on the host cores, bounded sample of the same workload per step."""
+    """--impl reference: the reference's CPU path (oracle port of its kernels, all host cores;
+    Julia is not installed) on the same workload; each step times a bounded sample (the next
+    slice of the instruction list plus one of expectation / probabilities / one shot) and the
+    line reports the whole-step rate extrapolated from the running means."""
     if rank != 0:
         return
-    import oracle
-    oracle.lib()
-    vals = []
+    ops = dense_circuit(OracleCircuit, n=N_QUBITS)
+    rs = ReferenceSampler(OracleCircuit, ops)
+    workload_bytes = len(ops) * 32.0 * 2 ** N_QUBITS
+    rs.sample(n_gates=8, parts=("expectation", "probabilities", "shot"))
+    vals, dts = [], []
     for i in range(args.warmup + args.steps):
-        res, dt = cpu_baseline_port(seconds_budget=8.0)
+        t0 = time.perf_counter()
+        rs.sample(n_gates=8)
+        dt = time.perf_counter() - t0
         if i >= args.warmup:
-            vals.append((res, dt))
-    v = float(np.mean([r["value"] for r, _ in vals]))
-    line = {"impl": "reference", "metric": "30q SV gate-layer HBM GB/s", "value": round(v, 2), "unit": "GB/s",
+            t_step, parts = rs.estimate()
+            vals.append(workload_bytes / t_step / 1e9)
+            dts.append(dt)
+    t_step, parts = rs.estimate()
+    v = float(vals[-1])
+    line = {"impl": "reference", "metric": "30q SV gate-layer HBM GB/s", "value": round(v, 3), "unit": "GB/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(1000 * float(np.mean([dt for _, dt in vals])), 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64)", "data": "synthetic",
-            "config": {"workload": workload_name(),
-                       "qubits": N_QUBITS, "shots": SHOTS,
-                       "bytes": "gate-layer bytes: 2*16*2^n per gate (one pass per gate, as the reference runs)",
-                       "sample": "each step times a bounded run of the workload's gate sweeps (SU(2) and CZ "
-                                 "passes of the reference kernels); GB/s per gate pass is the same unit"},
-            "cpu_baseline": {**vals[-1][0], "value": round(v, 2)},
-            "e2e": {"value": round(v, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "ms_per_step": round(1000 * float(np.mean(dts)), 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64)", "data": "synthetic (seeded Haar SU(2) + CZ)",
+            "config": workload_config(world, len(ops)),
+            "extrapolated_s_per_step": round(t_step, 1),
+            "parts_s": {k: round(x, 2) for k, x in parts.items()},
+            "evolve_only_GBps": round(workload_bytes / parts["evolve"] / 1e9, 2),
+            "ms_per_step_note": "host time of each step's bounded sample; value uses extrapolated_s_per_step",
+            "cpu_baseline": {"value": round(v, 3), "unit": "GB/s", "cores": rs.cores, "kind": "port",
+                             "sample": rs.describe()},
+            "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -560,22 +744,29 @@ def main():
     sweep_bytes = 32.0 * 2 ** N_QUBITS            # algorithmic HBM bytes of one sweep (read + write)
     if tc_launches:
         # dominant kernel: the tensor-core sweep, timed by the library with CUDA events around each launch
+        # on the stream it is launched on.  Its roofline is the sweep's algorithmic HBM bytes (one read and
+        # one write of the state, 2*16*2^n B per launch); the tensor work it executes is reported beside it.
         tc_launch_s = tc_ms * 1e-3 / tc_launches
-        flop_per_launch = tc_gates * 2 ** (N_QUBITS - 12) * TC_FLOP_PER_TILE_GATE / tc_launches
-        tflops = flop_per_launch / tc_launch_s / 1e12
         hbm_gbs = sweep_bytes / tc_launch_s / 1e9
-        roofline = {"bound": "tensor", "achieved": round(tflops, 1), "peak": bf16, "unit": "TFLOP/s",
-                    "frac": round(tflops / bf16, 3), "traffic": round(TC_DRAM_BYTES_PER_AMP * 2 ** N_QUBITS),
-                    "peak_source": f"{src} (bf16 sustained)", "kernel": "k_tile_sweep_tc",
-                    "flop_per_launch": flop_per_launch, "launch_ms": round(tc_launch_s * 1e3, 2),
+        flop_per_launch = tc_gates * 2 ** (N_QUBITS - 12) * TC_FLOP_PER_TILE_GATE / tc_launches
+        alg_flop_per_launch = tc_gates * 2 ** N_QUBITS * 256.0 / tc_launches
+        roofline = {"bound": "hbm", "achieved": round(hbm_gbs, 1), "peak": hbm, "unit": "GB/s",
+                    "frac": round(hbm_gbs / hbm, 3), "traffic": round(TC_DRAM_BYTES_PER_AMP * 2 ** N_QUBITS),
+                    "peak_source": f"{src} (HBM copy)", "kernel": "k_tile_sweep_tc",
+                    "bytes_per_launch": sweep_bytes, "launch_ms": round(tc_launch_s * 1e3, 2),
                     "launches_per_step": tc_launches // args.steps,
-                    "hbm_view": {"achieved": round(hbm_gbs, 1), "peak": hbm, "unit": "GB/s",
-                                 "frac": round(hbm_gbs / hbm, 3), "bytes_per_launch": sweep_bytes}}
+                    "fused_unitaries_per_launch": round(tc_gates / tc_launches, 2),
+                    "tensor_view": {
+                        "executed_bf16_TFLOPs": round(flop_per_launch / tc_launch_s / 1e12, 1),
+                        "executed_frac_of_bf16_sustained": round(flop_per_launch / tc_launch_s / 1e12 / bf16, 3),
+                        "algorithmic_TFLOPs": round(alg_flop_per_launch / tc_launch_s / 1e12, 2),
+                        "note": "executed = 26 bf16 digit-pair MMAs per complex128 product (exact split); "
+                                "algorithmic = 256 flop per amplitude per fused 5-qubit unitary"}}
     else:
         per_launch_ms = dev_ms / max(1, sweeps)
         achieved = sweep_bytes / (per_launch_ms * 1e-3) / 1e9
         roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                    "frac": round(achieved / hbm, 3), "traffic": None, "peak_source": src,
+                    "frac": round(achieved / hbm, 3), "traffic": None, "peak_source": f"{src} (HBM copy)",
                     "kernel": "k_tile_sweep", "bytes_per_launch": sweep_bytes}
     # value: the workload's gate-layer bytes (2*16*2^n per gate: the one pass per gate the reference
     # makes) over the device time, so that it compares with the reference arm's number for the same
@@ -590,10 +781,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * wall / args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c128 state, float-float (FP32-pipe) arithmetic", "data": "synthetic (seeded Haar SU(2) + CZ)",
-        "config": {"workload": workload_name(),
-                   "qubits": N_QUBITS, "gates": n_gates, "shots": SHOTS,
-                   "bytes": "gate-layer bytes: 2*16*2^n per gate (one pass per gate, as the reference runs)",
-                   "l2": l2_note(), "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "config": workload_config(world, n_gates),
         "e2e": {"value": round(e2e, 1), "unit": "GB/s", "h2d_bytes_per_step": int(n_gates * 64 + 200 * n_gates),
                 "d2h_bytes_per_step": int(SHOTS * 8 + 8)},
         "roofline": roofline,
@@ -604,8 +792,9 @@ def main():
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
+    line["check"] = headline_check(bs, sim, ops, e)
     if not args.no_cpu:
-        line["cpu_baseline"], _ = cpu_baseline_port()
+        line["cpu_baseline"] = cpu_baseline_reference(OracleCircuit, dense_circuit(OracleCircuit, n=N_QUBITS))
     if not args.no_adjoint:
         line["adjoint"] = adjoint_bench(bs)
         line["adjoint240"] = adjoint_bench(bs, ansatz="ry_cz", c64=False)   # the 240-parameter ansatz

@@ -15,7 +15,6 @@
 // race on it and must be serialised by the caller.  Each call clears the part it
 // accumulates into before using it.
 #include <cstring>
-#include <mutex>
 #include "bs_internal.h"
 #include "bs_ff.cuh"
 
@@ -121,20 +120,14 @@ __global__ void k_noalloc_finish(const double* __restrict__ partial, int nblocks
     }
 }
 
-std::mutex g_setup_mu;
-double* g_scratch_dev[64] = {nullptr};
-
-// Resolve the device address of the static array for the current device (once).
+// Device address of the static array in the current device's context.  Looked up on every
+// call rather than cached: the lookup allocates nothing, and a cached address would go stale
+// once a caller resets the device (cudaDeviceReset) and the library's module is loaded again
+// into the new context.  The first lookup on a device loads the library's device code.
 int scratch_for_current_device(double** out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return BS_ERR_CUDA;
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_dev[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return BS_ERR_CUDA;
-        g_scratch_dev[dev] = static_cast<double*>(p);
-    }
-    *out = g_scratch_dev[dev];
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return BS_ERR_CUDA;
+    *out = static_cast<double*>(p);
     return BS_OK;
 }
 

@@ -180,9 +180,11 @@ int bs_adjoint_gradient(bs_sim* sim, const bs_op* ops, int64_t n_ops, const int3
  * Scratch: one static 256 KiB device array inside the library, present on every GPU that
  * loads it until the process exits; no cudaMalloc/cudaFree or other allocation is made.
  * Limits: n_terms <= 32 and n_qubits <= 34 (SV) / 17 (DM); larger requests return
- * BS_ERR_UNSUPPORTED.  The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress) and should come before any stream capture.  Every call reuses the
- * same array, so calls that can overlap on the GPU race and must be serialised by the caller. */
+ * BS_ERR_UNSUPPORTED.  Every call looks up the array's device address on the current device
+ * (cudaGetSymbolAddress, which allocates nothing, so the address stays right after a caller's
+ * cudaDeviceReset); the first call on each device also loads the library's device code and
+ * should come before any stream capture.  Every call reuses the same array, so calls that can
+ * overlap on the GPU race and must be serialised by the caller. */
 int bs_expectation_pauli_noalloc(const void* state_dev, int kind, int n_qubits, int n_terms,
                                  const uint64_t* xmask, const uint64_t* zmask, const double* coeffs,
                                  double* out, void* stream);

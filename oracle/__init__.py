@@ -66,6 +66,8 @@ def lib():
             getattr(L, name).restype = None
         L.orc_pairwise_sum.argtypes = [P, I64]
         L.orc_pairwise_sum.restype = D
+        L.orc_expect_pauli.argtypes = [P, I64, C.c_uint64, C.c_uint64, I]
+        L.orc_expect_pauli.restype = D
         _lib = L
     return _lib
 
@@ -558,3 +560,77 @@ def expectation_pauli_dm(rho, n, xmask, zmask):
             apply_gate(_Fake(g, (), 1.0), s, [q])
     d = 2 ** n
     return float(np.real(np.sum(s[:: d + 1])))
+
+
+def expectation_pauli_fast(psi, n, xmask, zmask):
+    """Same number as expectation_pauli_sv (bit q <-> qubit q), from the one-pass C kernel."""
+    xi = zi = 0
+    ny = 0
+    for q in range(n):
+        x, z = (xmask >> q) & 1, (zmask >> q) & 1
+        if x:
+            xi |= 1 << (n - 1 - q)
+        if z:
+            zi |= 1 << (n - 1 - q)
+        ny += int(x and z)
+    psi = np.ascontiguousarray(psi, dtype=np.complex128)
+    return lib().orc_expect_pauli(_p(psi), psi.size, xi, zi, ny)
+
+
+# ---------------------------------------------------------------------------- gradients
+# The reference has no gradient (AdjointGradient is declared in src/results.jl:90-159 and
+# rejected in src/pragmas.jl:67-68).  Its users differentiate by the parameter-shift rule:
+# two forward simulations per parameter.  That is restated here on the oracle's FP64
+# simulator as the checker for the engine's adjoint gradients.  For a gate exp(-i phi G / 2)
+# with G^2 = 1 (Rx, Ry, Rz, XX, YY, ZZ; PhaseShift = e^{i phi/2} Rz(phi)), the rule is exact:
+#   dE/dphi = [E(phi + pi/2) - E(phi - pi/2)] / 2,
+# and a gate raised to pow_exponent p has phi = p * theta, so dE/dtheta = p * dE/dphi.
+SHIFT_GATES = ("rx", "ry", "rz", "xx", "yy", "zz", "phaseshift")
+
+
+class _Ix:
+    def __init__(self, operator, target):
+        self.operator, self.target = operator, list(target)
+
+
+def _is_param(ix):
+    return _gate_desc(ix.operator)[0] in SHIFT_GATES
+
+
+def hamiltonian_energy(psi, n, hamiltonian):
+    """sum_t c_t <psi|P_t|psi> for terms (c_t, {qubit: 'X'|'Y'|'Z'})."""
+    e = 0.0
+    for c, term in hamiltonian:
+        x = sum(1 << int(q) for q, p in term.items() if p.upper() in "XY")
+        z = sum(1 << int(q) for q, p in term.items() if p.upper() in "YZ")
+        e += float(c) * expectation_pauli_fast(psi, n, x, z)
+    return e
+
+
+def parameter_shift_gradient(n, instructions, hamiltonian, which=None):
+    """(energy, {instruction index: dE/dtheta}) on the FP64 oracle from |0...0>.
+
+    which: instruction indices to differentiate (default: every Rx/Ry/Rz/XX/YY/ZZ/PhaseShift).
+    The state before each chosen gate is carried forward once, so the cost is one full
+    forward pass plus two suffix passes per parameter."""
+    ins = list(instructions)
+    idx = [i for i, ix in enumerate(ins) if _is_param(ix)] if which is None else sorted(int(i) for i in which)
+    sv = OracleSV(n)
+    pos = 0
+    grads = {}
+    for i in idx:
+        sv.evolve(ins[pos:i])
+        pos = i
+        name, ang, pw = _gate_desc(ins[i].operator)
+        if name not in SHIFT_GATES:
+            raise ValueError(f"instruction {i} ({name}) has no two-term shift rule")
+        vals = []
+        for sgn in (1.0, -1.0):
+            s = OracleSV(n)
+            s.psi = sv.psi.copy()
+            shifted = _Ix(_Fake(name, (ang[0] + sgn * (math.pi / 2) / pw,), pw), ins[i].target)
+            s.evolve([shifted] + ins[i + 1:])
+            vals.append(hamiltonian_energy(s.psi, n, hamiltonian))
+        grads[i] = pw * (vals[0] - vals[1]) / 2.0
+    sv.evolve(ins[pos:])
+    return hamiltonian_energy(sv.psi, n, hamiltonian), grads

@@ -350,3 +350,31 @@ void orc_sample_direct(const double* w, int64_t n, double wsum, const double* u,
         out[s] = i;
     }
 }
+
+/* ---------------- Pauli expectations in one pass ---------------- */
+
+/* <psi|P|psi> for a Pauli string P, evaluated in one read of psi.  The reference
+ * computes the same number by applying the observable's gates to a copy of psi and
+ * taking real(dot(psi, copy)) (src/sv_simulator.jl:240-248, src/result_types.jl:196-221);
+ * a Pauli string acts on basis state i as
+ *   (P psi)_i = (-i)^{#Y} (-1)^{popcount(i & zidx)} psi_{i ^ xidx},
+ * with xidx / zidx the index bits of the X-or-Y / Z-or-Y factors (qubit q <-> bit n-1-q).
+ * Used for the oracle's parameter-shift gradients, where the apply-then-dot form would
+ * cost one sweep per factor per term. */
+double orc_expect_pauli(const cplx* psi, int64_t n_amps, uint64_t xidx, uint64_t zidx, int n_y) {
+    double re = 0.0, im = 0.0;
+#pragma omp parallel for reduction(+:re, im) schedule(static) if (n_amps >= ORC_PAR_MIN)
+    for (int64_t i = 0; i < n_amps; i++) {
+        cplx v = conj(psi[i]) * psi[i ^ (int64_t)xidx];
+        if (__builtin_popcountll((uint64_t)i & zidx) & 1) v = -v;
+        re += creal(v);
+        im += cimag(v);
+    }
+    /* multiply by (-i)^{n_y} and keep the real part */
+    switch (n_y & 3) {
+        case 0: return re;
+        case 1: return im;      /* (-i)(re + i im) = im - i re */
+        case 2: return -re;
+        default: return -im;    /* (i)(re + i im) = -im + i re */
+    }
+}
