@@ -296,6 +296,38 @@ def headline_check(bs, sim, ops, zz):
             "mirror_err": mirror, "tol": 1e-12, "checked": bool(mirror < 1e-12 and abs(zz - zz_ff) < 1e-12)}
 
 
+def dense_cnot_bench(bs, reps=2):
+    """Side measurement: the same 30-qubit circuit with CNOT in place of CZ, a dense 2-qubit gate
+    that fusion cannot fold into a parity phase (strides 8 and 16 included), timed like the headline
+    evolution, with the mirror check (the inverse circuit gives back |0...0>)."""
+    import torch
+    ops = dense_circuit(bs, n=N_QUBITS, two_qubit="cnot")
+    sim = bs.StateVectorSimulator(N_QUBITS, 0)
+    sim.evolve(ops)
+    torch.cuda.synchronize()
+    ms, st = [], None
+    for _ in range(reps):
+        sim.reinit(N_QUBITS, 0)
+        sim.evolve(ops)
+        st = sim.last_stats()
+        ms.append(st["gpu_ms"])
+    hbm, _, _ = peaks()
+    sweep_bytes = 32.0 * 2 ** N_QUBITS
+    dev = float(np.median(ms))
+    out = {"gates": len(ops), "evolve_ms": round(dev, 1), "sweeps": st["sweeps"],
+           "tensor_core_fused_unitaries": st["tc_gates"], "gate_layer_GBps": round(len(ops) * sweep_bytes / dev / 1e6, 1),
+           "executed_sweep_GBps": round(st["bytes_moved"] / dev / 1e6, 1)}
+    if st["tc_launches"]:
+        launch_s = st["tc_ms"] * 1e-3 / st["tc_launches"]
+        out["k_tile_sweep_tc"] = {"launch_ms": round(launch_s * 1e3, 2), "launches": st["tc_launches"],
+                                  "hbm_frac": round(sweep_bytes / launch_s / 1e9 / hbm, 3)}
+    sim.evolve(inverse_circuit(bs, ops))
+    psi = sim.state_vector
+    out["mirror_err"] = float(np.sqrt(abs(psi[0] - 1.0) ** 2 + np.vdot(psi[1:], psi[1:]).real))
+    out["checked"] = bool(out["mirror_err"] < 1e-12)
+    return out
+
+
 def cpu_baseline_reference(bs, ops, budget_s=25.0):
     """cpu_baseline for the headline line: a bounded sample (about budget_s of host work)."""
     rs = ReferenceSampler(bs, ops)
@@ -395,11 +427,21 @@ def adjoint_bench(bs, n=24, layers=10, terms=48, shift_params=24, seed=3, ansatz
                     "energy_diff_vs_c128": float(abs(e64 - e))}}
 
 
-def ghz_bench(bs, reps=100, cpu=False):
-    """GHZ-10 (H, CNOT(0,k)), full probabilities and 1000 shots per circuit: latency-bound."""
+def ghz_bench(bs, reps=200, cpu=False):
+    """GHZ-10 (H, CNOT(0,k)), full probabilities and 1000 shots per circuit: latency-bound.
+    run(): simulate in one round trip (one upload, one CTA for the whole circuit, the sampler, one
+    copy back); four_calls: reinit, evolve, probabilities and samples as separate calls."""
     import torch
     ops = [bs.Instruction(bs.H(), [0])] + [bs.Instruction(bs.CNot(), [0, k]) for k in range(1, 10)]
     sim = bs.StateVectorSimulator(10, 1000)
+    for r in range(10):
+        sim.run(ops, 1000, seed=r)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in range(reps):
+        p, s = sim.run(ops, 1000, seed=r)
+    dt = (time.perf_counter() - t0) / reps
+    ok = abs(p[0] - 0.5) < 1e-15 and abs(p[-1] - 0.5) < 1e-15 and set(np.unique(s)) <= {0, 1023}
     for r in range(5):
         sim.reinit(10, 1000)
         sim.evolve(ops)
@@ -410,12 +452,13 @@ def ghz_bench(bs, reps=100, cpu=False):
     for r in range(reps):
         sim.reinit(10, 1000)
         sim.evolve(ops)
-        p = sim.probabilities()
-        s = sim.samples(r)
-    torch.cuda.synchronize()
-    dt = (time.perf_counter() - t0) / reps
-    ok = abs(p[0] - 0.5) < 1e-15 and abs(p[-1] - 0.5) < 1e-15 and set(np.unique(s)) <= {0, 1023}
-    out = {"us_per_circuit": round(dt * 1e6, 1), "circuits_per_s": round(1 / dt, 1), "checked": bool(ok)}
+        p4 = sim.probabilities()
+        s4 = sim.samples(r)
+    dt4 = (time.perf_counter() - t0) / reps
+    ok = ok and np.array_equal(p4, p) and np.array_equal(s4, s)
+    out = {"us_per_circuit": round(dt * 1e6, 1), "circuits_per_s": round(1 / dt, 1),
+           "api": "StateVectorSimulator.run (bs_run_small)", "four_calls_us_per_circuit": round(dt4 * 1e6, 1),
+           "checked": bool(ok)}
     if cpu:
         out["cpu_baseline"] = ghz_cpu_port(reps)
     return out
@@ -488,16 +531,20 @@ def dm_bench(bs, n=14, cpu=False):
         dt = time.perf_counter() - t0
         out[mode] = {"s_per_circuit": round(dt, 3), "evolve_gpu_ms": round(st["gpu_ms"], 1), "sweeps": st["sweeps"],
                      "sweep_GBps": round(st["bytes_moved"] / (st["gpu_ms"] * 1e-3) / 1e9, 1),
-                     "trace": round(float(np.sum(diag)), 12), "x4": ex}
+                     "trace": float(np.sum(diag)), "x4": ex}
     out["instructions"] = len(ops)
     if cpu:
-        out["cpu_baseline"] = dm_cpu_port(ops, n)
+        out["cpu_baseline"] = cb = dm_cpu_port(ops, n)
+        if "oracle_x4" in cb:
+            out["reference"]["x4_abs_diff_vs_oracle"] = abs(out["reference"]["x4"] - cb["oracle_x4"])
+            out["reference"]["trace_abs_diff_vs_oracle"] = abs(out["reference"]["trace"] - cb["oracle_trace"])
     return out
 
 
-def dm_cpu_port(ops, n=14, depth=12):
-    """Reference noise mode on the oracle port of the reference's CPU kernels (all host threads):
-    the first of the circuit's `depth` identical-shape layers is timed and scaled by `depth`."""
+def dm_cpu_port(ops, n=14, depth=12, budget_s=40.0):
+    """Reference noise mode on the oracle port of the reference's CPU kernels (all host threads),
+    layer by layer: the whole circuit when it fits the budget (then the oracle's trace and <X X X X>
+    are returned beside the time, as the checker of the GPU values), else the layers done, scaled."""
     import oracle
     oracle.lib()
     layer = len(ops) // depth
@@ -505,10 +552,21 @@ def dm_cpu_port(ops, n=14, depth=12):
     sim.rho[:] = 0
     sim.rho[0] = 1.0
     t0 = time.perf_counter()
-    sim.evolve(ops[:layer])
+    done = 0
+    while done < depth:
+        sim.evolve(ops[done * layer:(done + 1) * layer])
+        done += 1
+        el = time.perf_counter() - t0
+        if el / done * depth > budget_s:
+            break
     dt = time.perf_counter() - t0
-    return {"s_per_circuit": round(dt * depth, 2), "cores": os.cpu_count(), "kind": "port",
-            "sample": f"1 of {depth} layers ({layer} instructions, {dt:.1f} s) timed, scaled by {depth}"}
+    out = {"s_per_circuit": round(dt * depth / done, 2), "cores": os.cpu_count(), "kind": "port",
+           "sample": f"{done} of {depth} layers ({done * layer} instructions, {dt:.1f} s) timed"
+                     + ("" if done == depth else f", scaled by {depth}/{done}")}
+    if done == depth:
+        out["oracle_trace"] = float(np.real(np.sum(sim.probabilities())))
+        out["oracle_x4"] = oracle.expectation_pauli_dm(sim.rho, n, 0b1111, 0)
+    return out
 
 
 def batch_circuits(bs, nc=512, seed=7):
@@ -574,22 +632,24 @@ def batch_bench(bs, cpu=False):
             "shots_each": 1000, "expectations_each": 8, "precision": "c64 (FP64 reductions)",
             "s_per_batch": round(dt, 3), "circuits_per_s": round(len(circuits) / dt, 1),
             "device_ms": round(st["gpu_ms"], 1), "sweeps": st["sweeps"],
-            "max_abs_err_c64_vs_c128_expectations": err,
+            "max_abs_err_c64_vs_engine_c128_expectations": err,
             "graph": {"capture_s": round(t_cap, 3), "s_per_replay": round(t_rep, 3),
                       "circuits_per_s": round(len(circuits) / t_rep, 1), "device_ms": round(st2["gpu_ms"], 1),
                       "replay_equals_one_shot": same},
-            **({"cpu_baseline": batch_cpu_port(circuits, counts)} if cpu else {})}
+            **({"cpu_baseline": batch_cpu_port(circuits, counts, obs, exp)} if cpu else {})}
 
 
-def batch_cpu_port(circuits, counts, budget_s=8.0):
+def batch_cpu_port(circuits, counts, obs=None, exp=None, budget_s=8.0):
     """The batch's gate sweeps on the oracle port of the reference's CPU kernels (complex128, all host
     threads; the reference has no complex64 path): circuits in batch order are evolved until the
-    budget is spent, and the whole batch's time is scaled from the sample by gate-sweep bytes."""
+    budget is spent, and the whole batch's time is scaled from the sample by gate-sweep bytes.  With
+    the GPU's complex64 expectations (exp) the oracle's complex128 values of the sampled circuits
+    check them."""
     import oracle
     oracle.lib()
     total = sum(len(c) * 32.0 * 2 ** n for c, n in zip(circuits, counts))
-    done_bytes, t_used, k = 0.0, 0.0, 0
-    for c, n in zip(circuits, counts):
+    done_bytes, t_used, k, errs = 0.0, 0.0, 0, []
+    for ci, (c, n) in enumerate(zip(circuits, counts)):
         if t_used > budget_s or n > 24:
             continue
         sim = oracle.OracleSV(n)
@@ -598,10 +658,19 @@ def batch_cpu_port(circuits, counts, budget_s=8.0):
         t_used += time.perf_counter() - t0
         done_bytes += len(c) * 32.0 * 2 ** n
         k += 1
+        if obs is not None and exp is not None:
+            for t, term in enumerate(obs[ci]):
+                x = sum(1 << q for q, pp in term.items() if pp in "XY")
+                z = sum(1 << q for q, pp in term.items() if pp in "YZ")
+                errs.append(abs(float(exp[ci, t]) - oracle.expectation_pauli_fast(sim.psi, n, x, z)))
     est = total / (done_bytes / t_used)
-    return {"circuits_per_s": round(len(circuits) / est, 2), "s_per_batch": round(est, 1), "cores": os.cpu_count(),
-            "kind": "port", "sample": f"{k} circuits of <=24 qubits evolved in {t_used:.1f} s; the batch scaled by "
-                                      "gate-sweep bytes (2*16*2^n per gate); shots and expectations not included"}
+    out = {"circuits_per_s": round(len(circuits) / est, 2), "s_per_batch": round(est, 1), "cores": os.cpu_count(),
+           "kind": "port", "sample": f"{k} circuits of <=24 qubits evolved in {t_used:.1f} s; the batch scaled by "
+                                     "gate-sweep bytes (2*16*2^n per gate); shots and expectations not included"}
+    if errs:
+        out["max_abs_err_gpu_c64_vs_oracle_c128"] = float(max(errs))
+        out["checked_expectations"] = len(errs)
+    return out
 
 
 def max_over_ranks(vals, world, device="cuda"):
@@ -796,6 +865,7 @@ def main():
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_reference(OracleCircuit, dense_circuit(OracleCircuit, n=N_QUBITS))
     if not args.no_adjoint:
+        line["dense_cnot"] = dense_cnot_bench(bs)
         line["adjoint"] = adjoint_bench(bs)
         line["adjoint240"] = adjoint_bench(bs, ansatz="ry_cz", c64=False)   # the 240-parameter ansatz
         line["ghz10"] = ghz_bench(bs, cpu=not args.no_cpu)

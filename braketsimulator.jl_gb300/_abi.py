@@ -19,6 +19,7 @@ BS_GATE_SORTED_TARGETS = 0x04
 BS_GATE_MSB_FIRST = 0x08
 BS_NOISE_REFERENCE = 0x00
 BS_NOISE_PHYSICAL = 0x10
+BS_ALIAS_EXACT, BS_ALIAS_PARALLEL = 0x0, 0x1
 BS_TUNE_TILE_BITS, BS_TUNE_TILE_THREADS, BS_TUNE_TC, BS_TUNE_TC_MIN_BITS, BS_TUNE_TC_COST = 0, 1, 2, 3, 4
 BS_TUNE_ADJ_SEGMENTS = 5
 BS_FILE_STATE, BS_FILE_PROBABILITIES = 0, 1
@@ -81,6 +82,7 @@ SIGNATURES = {
     "bs_dm_apply_vec_gate": (_i32, [_p, _P(_f64), _i32, _P(_i32), _i32, _P(_i32), _P(_i32), _u32]),
     "bs_apply_kraus": (_i32, [_p, _P(_f64), _i32, _i32, _P(_i32), _u32]),
     "bs_evolve": (_i32, [_p, _P(BsOp), _i64, _u32]),
+    "bs_run_small": (_i32, [_p, _P(BsOp), _i64, _i64, _u64, _P(_f64), _P(_i64)]),
     "bs_last_stats": (_i32, [_p, _P(BsStats)]),
     "bs_probabilities": (_i32, [_p, _P(_f64), _i64]),
     "bs_marginal_probabilities": (_i32, [_p, _i32, _P(_i32), _P(_f64)]),

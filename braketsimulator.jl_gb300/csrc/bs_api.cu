@@ -461,6 +461,10 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
         std::vector<Sweep> sw;
         bs_plan_sweeps(pending, bs_vec_bits(s), bs_tile_bits(s), sw);
         pending.clear();
+        if (s->collect) {   // bs_run_small: plan only
+            s->collect->insert(s->collect->end(), sw.begin(), sw.end());
+            return BS_OK;
+        }
         return bs_run_sweeps(s, sw);
     };
     const bool dm = s->kind == BS_KIND_DM;
@@ -509,6 +513,69 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     s->stats.gpu_ms = ms;
     bs_collect_tc_time(s);
     return bs_check_device_flag(s);
+}
+
+// simulate (src/BraketSimulator.jl:307-322: reinit!, evolve!, probabilities, samples) of one small
+// state-vector circuit as one upload, two launches and one synchronisation.
+int bs_run_small(bs_sim* s, const bs_op* ops, int64_t n_ops, int64_t shots, uint64_t seed, double* probs_out,
+                 int64_t* samples_out) {
+    if (!s) return BS_ERR_INVALID_ARG;
+    if (s->kind != BS_KIND_SV || s->n > 12) return bs_fail(s, BS_ERR_UNSUPPORTED, "bs_run_small: state vectors of at most 12 qubits");
+    if (s->capturing) return bs_fail(s, BS_ERR_STATE, "bs_run_small: not during graph capture");
+    if (shots < 0 || (shots > 0 && !samples_out)) return bs_fail(s, BS_ERR_INVALID_ARG, "bad shot buffer");
+    const int64_t dim = (int64_t)1 << s->n;
+    std::vector<Sweep> sweeps;
+    // plan the instruction list as bs_evolve does (lowering, SWAP relabelling, diagonal folding), launching nothing
+    s->collect = &sweeps;
+    const bool defer = s->defer_sync;
+    s->defer_sync = true;
+    int rc = bs_evolve(s, ops, n_ops, BS_NOISE_REFERENCE);
+    s->defer_sync = defer;
+    s->collect = nullptr;
+    if (rc) return rc;
+    rc = bs_ensure_scratch(s, dim * 8 + shots * 8 + 256);
+    if (rc) return rc;
+    double* dprobs = (double*)s->scratch;
+    int64_t* dsamp = (int64_t*)((char*)s->scratch + ((dim * 8 + 255) & ~(int64_t)255));
+    cudaEventRecord(s->ev0, s->stream);
+    rc = bs_run_small_sweeps(s, sweeps, dprobs);
+    if (rc == BS_ERR_UNSUPPORTED) {
+        // a gate without an in-tile kernel (dense on more than 4 qubits) or a complex64 state: the usual
+        // path, with the same results
+        rc = bs_reinit(s, s->n);
+        if (!rc) rc = bs_evolve(s, ops, n_ops, BS_NOISE_REFERENCE);
+        if (!rc && probs_out) rc = bs_probabilities(s, probs_out, dim);
+        if (!rc && shots > 0) rc = bs_sample(s, seed, shots, samples_out);
+        return rc;
+    }
+    if (rc) return rc;
+    s->alias_valid = false;
+    if (shots > 0) {
+        rc = bs_launch_sample_small(s, seed, shots, dsamp);
+        if (rc) return rc;
+    }
+    cudaEventRecord(s->ev1, s->stream);
+    // results: one copy of [probabilities | samples] through the pinned per-thread buffer when it fits
+    const size_t pb = probs_out ? (size_t)dim * 8 : 0, sb = (size_t)shots * 8;
+    if (pb + sb <= kOutStage && (t_out.p || cudaMallocHost(&t_out.p, kOutStage) == cudaSuccess)) {
+        if (pb) cudaMemcpyAsync(t_out.p, dprobs, pb, cudaMemcpyDeviceToHost, s->stream);
+        if (sb) cudaMemcpyAsync((char*)t_out.p + pb, dsamp, sb, cudaMemcpyDeviceToHost, s->stream);
+        rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "small run");
+        if (rc) return rc;
+        if (pb) std::memcpy(probs_out, t_out.p, pb);
+        if (sb) std::memcpy(samples_out, (char*)t_out.p + pb, sb);
+    } else {
+        cudaGetLastError();
+        if (pb) cudaMemcpyAsync(probs_out, dprobs, pb, cudaMemcpyDeviceToHost, s->stream);
+        if (sb) cudaMemcpyAsync(samples_out, dsamp, sb, cudaMemcpyDeviceToHost, s->stream);
+        rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "small run");
+        if (rc) return rc;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    s->stats.gpu_ms = ms;
+    s->stats_pending = false;
+    return BS_OK;
 }
 
 }  // extern "C"

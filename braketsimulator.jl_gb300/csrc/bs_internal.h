@@ -122,6 +122,7 @@ struct bs_sim {
     bool stats_pending = false;   // an evolve returned before its end event (ev1) completed
     std::vector<std::pair<char*, size_t>> arena;   // chunks (pointer, capacity)
     size_t arena_used = 0;                          // bytes used in the last chunk
+    std::vector<Sweep>* collect = nullptr;          // bs_evolve plans into this list instead of launching
 };
 
 // ---- helpers implemented in bs_api.cu
@@ -176,3 +177,15 @@ int bs_kraus_reference(bs_sim* s, const double* kraus, int nk, int k, const int*
 // The same channel (1 or 2 targets) as a kind-5 HostGate applied inside a sweep.
 int bs_lower_kraus_reference(bs_sim* s, const double* kraus, int nk, int k, const int* targets, unsigned flags,
                              std::vector<HostGate>& out);
+
+// ---- parallel alias table (bs_alias_par.cu)
+int64_t bs_alias_parallel_scratch(int64_t n);
+int bs_alias_parallel(bs_sim* s, const double* dprobs, int64_t n, double wsum, double* ap, int64_t* alias, void* work);
+
+// ---- small state vectors in one CTA (bs_tile.cu, bs_sample.cu)
+// |0...0>, the planned sweeps' gates, the state written back and its probabilities into dprobs (device);
+// BS_ERR_UNSUPPORTED (nothing launched) when a gate has no in-tile kernel or the state is not a
+// complex128 state vector of at most 12 qubits.
+int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dprobs);
+// k_sample_small's draws (bs_sample's generator) of a state of at most 4096 amplitudes into dout (device)
+int bs_launch_sample_small(bs_sim* s, uint64_t seed, int64_t shots, int64_t* dout);

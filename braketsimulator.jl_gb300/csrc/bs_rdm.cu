@@ -2,7 +2,9 @@
 //
 // Reference: partial_trace (src/sv_simulator.jl:273-318 for a state vector,
 // src/dm_simulator.jl:280-323 for a density matrix), reached through the
-// DensityMatrix result type (src/result_types.jl:239-246).  The reference loops
+// DensityMatrix result type (src/result_types.jl:239-246); keeping every qubit of a state vector
+// gives its density matrix psi psi^dagger (density_matrix, src/sv_simulator.jl:151-152).  The
+// reference loops
 // over the traced configurations on the host; here the sum runs in float-float on
 // the device and only the 2^k x 2^k result is copied back.
 //
@@ -20,6 +22,8 @@
 #include "bs_internal.h"
 #include "bs_ff.cuh"
 
+#define BS_RDM_MAX_KEEP 16   // a 2^16 x 2^16 complex128 result is 64 GiB
+
 namespace {
 
 constexpr int kRT = 256;    // threads per CTA
@@ -29,7 +33,7 @@ constexpr int kBB = 16;     // traced configurations staged per step
 struct RdmDesc {
     int n_bits;            // vector bits (n for SV; the matrix side n for DM)
     int k;                 // kept bits
-    int kbit[12];          // kept endian bits, ascending
+    int kbit[BS_RDM_MAX_KEEP];   // kept endian bits, ascending
     int64_t nb;            // traced configurations, 2^(n-k)
     int64_t per;           // configurations per chunk
     int ts;                // tile edge (<= 64)
@@ -153,7 +157,8 @@ __global__ void k_rdm_reduce(const float4* __restrict__ partial, RdmDesc d, int 
 
 extern "C" int bs_reduced_density_matrix(bs_sim* s, int n_keep, const int* qubits, double* out) {
     if (!s) return BS_ERR_INVALID_ARG;
-    if (n_keep < 1 || n_keep > 12 || !qubits || !out) return bs_fail(s, BS_ERR_INVALID_ARG, "keep 1..12 qubits");
+    if (n_keep < 1 || !qubits || !out) return bs_fail(s, BS_ERR_INVALID_ARG, "keep at least one qubit");
+    if (n_keep > BS_RDM_MAX_KEEP) return bs_fail(s, BS_ERR_UNSUPPORTED, "at most 16 kept qubits (a 64 GiB result)");
     if (n_keep > s->n) return bs_fail(s, BS_ERR_INVALID_ARG, "more kept qubits than the register has");
     uint64_t seen = 0;
     RdmDesc d{};

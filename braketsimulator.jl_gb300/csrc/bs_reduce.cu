@@ -236,6 +236,61 @@ __global__ void __launch_bounds__(kRThreads) k_marginal(const typename Elem<C64>
     for (int o = threadIdx.x; o < D; o += blockDim.x) partial[(int64_t)blockIdx.x * D + o] = hist[o];
 }
 
+// Marginals over more than 12 targets (no shared-memory histogram): out[o] = sum over the traced
+// configurations b of p(place(o, b)), in float-float, per (output, chunk of b); WARP: one warp per
+// output with its lanes over b (traced bits include the contiguous low ones), else one thread per
+// output.  partial[c * D + o] holds chunk c's sum (hi, lo).
+struct WideMarg {
+    int nbits;          // vector bits (qubits)
+    int k;              // kept bits
+    int kbit[64];       // kept endian bits, ascending (output bit q <-> kbit[q])
+    int64_t nb, per;    // traced configurations, per chunk
+};
+__device__ __forceinline__ int64_t wm_place(const WideMarg& d, int64_t o, int64_t b) {
+    int64_t g = b;
+    for (int q = 0; q < d.k; q++) {
+        const int p = d.kbit[q];
+        g = ((g >> p) << (p + 1)) | (g & (((int64_t)1 << p) - 1));
+    }
+    for (int q = 0; q < d.k; q++) g |= ((o >> q) & 1) << d.kbit[q];
+    return g;
+}
+template <bool C64, bool WARP>
+__global__ void __launch_bounds__(kRThreads) k_marginal_wide(const typename Elem<C64>::T* __restrict__ st, int dm,
+                                                             WideMarg d, float2* __restrict__ partial) {
+    const int64_t D = (int64_t)1 << d.k, dim = (int64_t)1 << d.nbits;
+    const int64_t c = blockIdx.y;
+    const int64_t b0 = c * d.per, b1 = std::min<int64_t>(d.nb, b0 + d.per);
+    const int lanes = WARP ? 32 : 1;
+    const int64_t o = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / lanes;
+    const int lane = WARP ? (threadIdx.x & 31) : 0;
+    if (o >= D) return;   // whole warps leave together (D is a multiple of the warp's outputs)
+    ffsum acc{0.f, 0.f};
+    for (int64_t b = b0 + lane; b < b1; b += lanes) {
+        const int64_t i = wm_place(d, o, b);
+        const double p = dm ? (double)st[i * (dim + 1)].x : prob_of<C64>(st[i]);
+        const ff f = d2ff(p);
+        fsum_add(acc, f.h, f.l);
+    }
+    if (WARP) {
+        for (int off = 16; off > 0; off >>= 1) {
+            const float h = __shfl_xor_sync(0xffffffffu, acc.h, off), l = __shfl_xor_sync(0xffffffffu, acc.l, off);
+            fsum_add(acc, h, l);
+        }
+    }
+    if (lane == 0) partial[c * D + o] = make_float2(acc.h, acc.l);
+}
+__global__ void k_marginal_wide_sum(const float2* __restrict__ partial, int64_t D, int64_t chunks, double* __restrict__ out) {
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < D; o += (int64_t)gridDim.x * blockDim.x) {
+        ffsum acc{0.f, 0.f};
+        for (int64_t c = 0; c < chunks; c++) {
+            const float2 v = partial[c * D + o];
+            fsum_add(acc, v.x, v.y);
+        }
+        out[o] = ff2d(acc.h, acc.l);
+    }
+}
+
 int grid_for(int64_t work) {
     int64_t b = (work + kRThreads - 1) / kRThreads;
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 8));
@@ -251,6 +306,41 @@ void launch_pauli(bs_sim* s, int nb, int64_t dim, uint64_t xm, const TermSet& se
 }
 
 }  // namespace
+
+// More than 12 targets: chunks of traced configurations so that about 152 x 2048 threads work,
+// float-float partial sums per chunk, then one pass over the chunks.
+static int marginal_wide(bs_sim* s, int k, const std::vector<int>& eb, double* host_out) {
+    WideMarg d{};
+    d.nbits = s->n;
+    d.k = k;
+    for (int q = 0; q < k; q++) d.kbit[q] = eb[(size_t)q];
+    const int64_t D = (int64_t)1 << k;
+    d.nb = (int64_t)1 << (s->n - k);
+    const bool warp = d.nb >= 32 && eb[0] != 0;     // lanes over b where the low bits are traced
+    const int64_t lanes = warp ? 32 : 1;
+    int64_t chunks = std::max<int64_t>(1, std::min<int64_t>(d.nb / lanes, (152LL * 2048) / (D * lanes) + 1));
+    chunks = std::min<int64_t>(chunks, 65535);
+    d.per = (d.nb + chunks - 1) / chunks;
+    chunks = (d.nb + d.per - 1) / d.per;
+    const int64_t pbytes = (chunks * D * 8 + 255) & ~(int64_t)255;
+    int rc = bs_ensure_scratch(s, pbytes + D * 8);
+    if (rc) return rc;
+    float2* partial = (float2*)s->scratch;
+    double* out = (double*)((char*)s->scratch + pbytes);
+    const dim3 grid((unsigned)((D * lanes + kRThreads - 1) / kRThreads), (unsigned)chunks);
+    const int dm = s->kind == BS_KIND_DM;
+    if (s->precision == BS_PREC_C64) {
+        if (warp) k_marginal_wide<true, true><<<grid, kRThreads, 0, s->stream>>>((const float2*)s->state, dm, d, partial);
+        else k_marginal_wide<true, false><<<grid, kRThreads, 0, s->stream>>>((const float2*)s->state, dm, d, partial);
+    } else {
+        if (warp) k_marginal_wide<false, true><<<grid, kRThreads, 0, s->stream>>>((const double2*)s->state, dm, d, partial);
+        else k_marginal_wide<false, false><<<grid, kRThreads, 0, s->stream>>>((const double2*)s->state, dm, d, partial);
+    }
+    k_marginal_wide_sum<<<grid_for(D), kRThreads, 0, s->stream>>>(partial, D, chunks, out);
+    rc = bs_cuda_check(s, cudaGetLastError(), "marginal");
+    if (rc) return rc;
+    return bs_copy_out(s, host_out, out, (size_t)D * 8, "marginal");
+}
 
 extern "C" {
 
@@ -371,7 +461,7 @@ int bs_expectation_matrix(bs_sim* s, const double* matrix, int k, const int* tar
 
 int bs_marginal_probabilities(bs_sim* s, int k, const int* targets, double* host_out) {
     if (!s) return BS_ERR_INVALID_ARG;
-    if (!targets || !host_out || k < 1 || k > 12 || k > s->n) return bs_fail(s, BS_ERR_INVALID_ARG, "marginal needs 1..12 targets");
+    if (!targets || !host_out || k < 1 || k > s->n) return bs_fail(s, BS_ERR_INVALID_ARG, "marginal needs 1..n targets");
     uint64_t seen = 0;
     for (int i = 0; i < k; i++) {
         if (targets[i] < 0 || targets[i] >= s->n) return bs_fail(s, BS_ERR_INVALID_ARG, "target qubit out of range");
@@ -381,6 +471,7 @@ int bs_marginal_probabilities(bs_sim* s, int k, const int* targets, double* host
     std::vector<int> eb(k);
     for (int j = 0; j < k; j++) eb[j] = s->n - 1 - targets[j];
     std::sort(eb.begin(), eb.end());
+    if (k > 12) return marginal_wide(s, k, eb, host_out);
     const int D = 1 << k;
     const int64_t dim = (int64_t)1 << s->n;
     const int nb = grid_for(dim);

@@ -327,13 +327,40 @@ int alias_from_device_probs(bs_sim* s, const double* dprobs, int64_t n, double w
 
 }  // namespace
 
+int bs_launch_sample_small(bs_sim* s, uint64_t seed, int64_t shots, int64_t* dout) {
+    const int64_t dim = (int64_t)1 << s->n;
+    if (dim > kBlk) return BS_ERR_UNSUPPORTED;
+    if (shots <= 0) return BS_OK;
+    const int mode = (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0);
+    const unsigned g = (unsigned)std::min<int64_t>(152, std::max<int64_t>(1, (shots + 15) / 16));
+    k_sample_small<<<g, 128, 0, s->stream>>>((const double2*)s->state, mode, dim, seed, shots, dout);
+    s->stats.kernel_launches++;
+    return bs_cuda_check(s, cudaGetLastError(), "sample");
+}
+
 extern "C" {
 
 int bs_alias_build(bs_sim* s, double wsum, unsigned flags) {
     if (!s) return BS_ERR_INVALID_ARG;
-    (void)flags;
+    if (flags & ~BS_ALIAS_PARALLEL) return bs_fail(s, BS_ERR_INVALID_ARG, "unknown alias flags");
     const int64_t dim = (int64_t)1 << s->n;
+    const int mode = (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0);
     int rc;
+    if (flags & BS_ALIAS_PARALLEL) {
+        // probabilities, then the parallel builder's work area 256 bytes further on; the builder
+        // takes the exact weight total itself when wsum is not given
+        rc = alias_alloc(s, dim);
+        if (rc) return rc;
+        const int64_t pbytes = (dim * 8 + 255) & ~(int64_t)255;
+        rc = bs_ensure_scratch(s, pbytes + bs_alias_parallel_scratch(dim));
+        if (rc) return rc;
+        double* p = (double*)s->scratch;
+        k_prob_any<<<grid(dim, 256), 256, 0, s->stream>>>((const double2*)s->state, mode, dim, p);
+        rc = bs_alias_parallel(s, p, dim, wsum, s->alias_ap, s->alias_ix, (char*)s->scratch + pbytes);
+        if (rc) return rc;
+        s->alias_valid = true;
+        return BS_OK;
+    }
     if (!(wsum > 0.0)) {
         // sum of the weights in float-float on the device (block sums + scan)
         double* incl = nullptr;
@@ -347,7 +374,7 @@ int bs_alias_build(bs_sim* s, double wsum, unsigned flags) {
     rc = bs_ensure_scratch(s, 3 * dim * 8 + 128);
     if (rc) return rc;
     double* p = (double*)s->scratch;
-    k_prob_any<<<grid(dim, 256), 256, 0, s->stream>>>((const double2*)s->state, (s->kind == BS_KIND_DM ? 1 : 0) | (s->precision == BS_PREC_C64 ? 2 : 0), dim, p);
+    k_prob_any<<<grid(dim, 256), 256, 0, s->stream>>>((const double2*)s->state, mode, dim, p);
     return alias_from_device_probs(s, p, dim, wsum);
 }
 

@@ -47,6 +47,9 @@ __device__ __forceinline__ cff f4c(float4 v) { return {v.x, v.z, v.y, v.w}; }
 __device__ __forceinline__ float4 c4f(const cff& c) { return make_float4(c.rh, c.ih, c.rl, c.il); }
 __device__ __forceinline__ cff f4m(float4 v) { return {v.x, v.y, v.z, v.w}; }
 
+// Dense gate on K tile bits in packed complex float-float (bs_ff.cuh: pacc): the real and
+// imaginary halves of each complex sum share one register pair, so one f32x2 instruction does the
+// work of two scalar ones, with the roundings of the scalar sequence in each half.
 template <int K, bool SW = false>
 __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* __restrict__ mats) {
     constexpr int D = 1 << K;
@@ -66,23 +69,31 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
 #pragma unroll
     for (int q = 0; q < K; q++) tb[q] = g.tbit[q];
     if (K == 1) {
-        // 2x2: matrix held in registers across the thread's pairs
-        const cff m00 = f4m(__ldg(m)), m01 = f4m(__ldg(m + 1)), m10 = f4m(__ldg(m + 2)), m11 = f4m(__ldg(m + 3));
+        // 2x2: packed coefficients held in registers across the thread's pairs
+        pcoef A[4], B[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) pcoefs(__ldg(m + e), A[e], B[e]);
         const int b0 = 1 << tb[0];
 #pragma unroll 2
         for (int gr = threadIdx.x; gr < ngroups; gr += blockDim.x) {
             const int jb = insert0(gr, pos[0]);
             if ((jb & (int)lcm) != (int)lcv) continue;
             const int ia = sx<SW>(jb), ib = sx<SW>(jb | b0);
-            const cff a = f4c(sm[ia]), b = f4c(sm[ib]);
-            ffacc ar, ai;
-            cmac_first(ar, ai, m00, a);
-            cmac(ar, ai, m01, b);
-            const cff ya = cdone(ar, ai);
-            cmac_first(ar, ai, m10, a);
-            cmac(ar, ai, m11, b);
-            sm[ib] = c4f(cdone(ar, ai));
-            sm[ia] = c4f(ya);
+            f2 ah, al, bh, bl;
+            split4(sm[ia], ah, al);
+            split4(sm[ib], bh, bl);
+            const f2 ash = swap2(ah), asl = swap2(al), bsh = swap2(bh), bsl = swap2(bl);
+            pacc y;
+            f2 yh, yl;
+            pcmac_first(y, A[0], B[0], ah, al, ash, asl);
+            pcmac(y, A[1], B[1], bh, bl, bsh, bsl);
+            pacc_done(y, yh, yl);
+            pcmac_first(y, A[2], B[2], ah, al, ash, asl);
+            pcmac(y, A[3], B[3], bh, bl, bsh, bsl);
+            f2 zh, zl;
+            pacc_done(y, zh, zl);
+            sm[ib] = join4(zh, zl);
+            sm[ia] = join4(yh, yl);
         }
         return;
     }
@@ -91,7 +102,7 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
 #pragma unroll
         for (int q = 0; q < K; q++) jb = insert0(jb, pos[q]);
         if ((jb & (int)lcm) != (int)lcv) continue;
-        cff x[D];
+        f2 xh[D], xl[D];
         int idx[D];
 #pragma unroll
         for (int c = 0; c < D; c++) {
@@ -99,15 +110,22 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
 #pragma unroll
             for (int q = 0; q < K; q++) if ((c >> q) & 1) j |= 1 << tb[q];
             idx[c] = sx<SW>(j);
-            x[c] = f4c(sm[idx[c]]);
+            split4(sm[idx[c]], xh[c], xl[c]);
         }
 #pragma unroll
         for (int r = 0; r < D; r++) {
-            ffacc ar, ai;
-            cmac_first(ar, ai, f4m(__ldg(m + r * D)), x[0]);
+            pacc y;
+            pcoef A, B;
+            pcoefs(__ldg(m + r * D), A, B);
+            pcmac_first(y, A, B, xh[0], xl[0], swap2(xh[0]), swap2(xl[0]));
 #pragma unroll
-            for (int c = 1; c < D; c++) cmac(ar, ai, f4m(__ldg(m + r * D + c)), x[c]);
-            sm[idx[r]] = c4f(cdone(ar, ai));
+            for (int c = 1; c < D; c++) {
+                pcoefs(__ldg(m + r * D + c), A, B);
+                pcmac(y, A, B, xh[c], xl[c], swap2(xh[c]), swap2(xl[c]));
+            }
+            f2 yh, yl;
+            pacc_done(y, yh, yl);
+            sm[idx[r]] = join4(yh, yl);
         }
     }
 }
@@ -196,7 +214,12 @@ __device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const flo
             if (d.x == 0.f && d.z == 1.f) { sm[js] = c4f(cmul_ipow(f4c(sm[js]), 1)); continue; }
             if (d.x == 0.f && d.z == -1.f) { sm[js] = c4f(cmul_ipow(f4c(sm[js]), 3)); continue; }
         }
-        sm[js] = c4f(cmul(f4m(d), f4c(sm[js])));
+        pcoef A, B;
+        pcoefs(d, A, B);
+        f2 xh, xl, yh, yl;
+        split4(sm[js], xh, xl);
+        pcmul(A, B, xh, xl, yh, yl);
+        sm[js] = join4(yh, yl);
     }
 }
 
@@ -1674,4 +1697,131 @@ int bs_check_device_flag(bs_sim* s) {
     if (rc) return rc;
     if (flag) return bs_fail(s, BS_ERR_TIMEOUT, "a tensor-core sweep gave up waiting for its copies or MMAs");
     return BS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Whole small state vectors in one CTA (bs_run_small): the reference's simulate of a small circuit
+// (src/BraketSimulator.jl:307-322: reinit!, evolve!, then results) as one launch.  The CTA builds
+// |0...0> in shared memory, applies every gate of the planned sweeps in order with the tile kernels'
+// float-float gates (the whole state is the tile, so sweep boundaries cost nothing), writes the state
+// back and the probabilities, computed from the stored complex128 values exactly as bs_probabilities
+// computes them.
+namespace {
+
+struct NoOff {
+    __device__ __forceinline__ int64_t operator[](int) const { return 0; }
+};
+
+template <int KMAX>
+__global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, int n, const TileGate* __restrict__ gates,
+                                                   int ng, const float4* __restrict__ mats,
+                                                   const int32_t* __restrict__ perms, double* __restrict__ probs) {
+    extern __shared__ float4 smem[];
+    const int nt = 1 << n;
+    for (int j = threadIdx.x; j < nt; j += blockDim.x) smem[j] = make_float4(j == 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    for (int gi = 0; gi < ng; gi++) {
+        const TileGate& g = gates[gi];
+        const int kind = g.kind, k = g.k;
+        if (kind == 0) {
+            if (k == 1) tile_dense<1>(smem, n, g, mats);
+            else if (k == 2) tile_dense<2>(smem, n, g, mats);
+            else if (KMAX == 4 && k == 3) tile_dense<3>(smem, n, g, mats);
+            else if (KMAX == 4) tile_dense<4>(smem, n, g, mats);
+        } else if (kind == 1) {
+            tile_diag<NoOff>(smem, n, n, g, mats, 0, NoOff{}, 0);
+        } else {
+            if (k == 1) tile_monomial<1>(smem, n, g, perms);
+            else if (k == 2) tile_monomial<2>(smem, n, g, perms);
+            else if (KMAX == 4 && k == 3) tile_monomial<3>(smem, n, g, perms);
+            else if (KMAX == 4) tile_monomial<4>(smem, n, g, perms);
+        }
+        __syncthreads();
+    }
+    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        const double2 v = store_c128(f4c(smem[j]));
+        psi[j] = v;
+        const cff x = load_c128(v);
+        ffacc a;
+        acc_first(a, x.rh, x.rl, x.rh, x.rl);
+        acc_add(a, x.ih, x.il, x.ih, x.il);
+        const ff r = acc_done(a);
+        probs[j] = ff2d(r.h, r.l);
+    }
+}
+
+}  // namespace
+
+int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dprobs) {
+    const int n = s->n;
+    if (s->kind != BS_KIND_SV || s->precision != BS_PREC_C128 || n > 12) return BS_ERR_UNSUPPORTED;
+    std::vector<TileGate> tg;
+    std::vector<float4> mats;
+    std::vector<int32_t> perms;
+    int kmax = 1;
+    for (const Sweep& sw : sweeps) {
+        std::vector<HostGate> merged;
+        merge_diagonals(sw.gates, merged);
+        for (const HostGate& hg : merged) {
+            if (hg.kind != 0 && hg.kind != 1 && hg.kind != 2) return BS_ERR_UNSUPPORTED;
+            if (hg.kind != 1 && hg.k > BS_TILE_MAXK) return BS_ERR_UNSUPPORTED;
+            TileGate t{};
+            t.kind = hg.kind;
+            t.k = hg.k;
+            t.lc_mask = (uint32_t)hg.cmask;   // every bit is in the tile, at its own position
+            t.lc_val = (uint32_t)hg.cval;
+            for (int q = 0; q < hg.k; q++) {
+                t.gbit[q] = hg.ebit[q];
+                if (q < BS_TILE_MAXK) t.tbit[q] = hg.ebit[q];
+            }
+            t.mat_off = (int32_t)mats.size();
+            t.perm_off = (int32_t)perms.size();
+            if (hg.kind == 0) {
+                for (int i = 0; i < (1 << (2 * hg.k)); i++) mats.push_back(to_cff(hg.mat[2 * i], hg.mat[2 * i + 1]));
+                kmax = std::max(kmax, hg.k);
+            } else if (hg.kind == 1) {
+                for (int i = 0; i < (1 << hg.k); i++) mats.push_back(to_cff(hg.mat[2 * i], hg.mat[2 * i + 1]));
+            } else {
+                perms.insert(perms.end(), hg.perm.begin(), hg.perm.end());
+                kmax = std::max(kmax, hg.k);
+            }
+            tg.push_back(t);
+        }
+    }
+    auto al = [](int64_t x) { return (x + 255) & ~(int64_t)255; };
+    const int64_t b_tg = al((int64_t)(tg.size() + 1) * (int64_t)sizeof(TileGate));
+    const int64_t b_m = al((int64_t)(mats.size() + 1) * (int64_t)sizeof(float4));
+    const int64_t b_p = al((int64_t)(perms.size() + 1) * (int64_t)sizeof(int32_t));
+    int rc = bs_ensure_plan(s, b_tg + b_m + b_p);
+    if (rc) return rc;
+    char* host = bs_stage(s, (size_t)(b_tg + b_m + b_p));
+    if (!host) return bs_fail(s, BS_ERR_ALLOC, "pinned staging allocation");
+    if (!tg.empty()) std::memcpy(host, tg.data(), tg.size() * sizeof(TileGate));
+    if (!mats.empty()) std::memcpy(host + b_tg, mats.data(), mats.size() * sizeof(float4));
+    if (!perms.empty()) std::memcpy(host + b_tg + b_m, perms.data(), perms.size() * sizeof(int32_t));
+    char* dev = (char*)s->plan_buf;
+    rc = bs_cuda_check(s, cudaMemcpyAsync(dev, host, (size_t)(b_tg + b_m + b_p), cudaMemcpyHostToDevice, s->stream),
+                       "plan upload");
+    bs_stage_done(s);
+    if (rc) return rc;
+    const size_t smem = ((size_t)1 << n) * sizeof(float4);
+    const TileGate* d_tg = (const TileGate*)dev;
+    const float4* d_m = (const float4*)(dev + b_tg);
+    const int32_t* d_p = (const int32_t*)(dev + b_tg + b_m);
+    static bool attr_set[64] = {false};
+    if (!attr_set[s->device & 63]) {
+        cudaFuncSetAttribute(k_small_run<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+        cudaFuncSetAttribute(k_small_run<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+        attr_set[s->device & 63] = true;
+    }
+    const int threads = std::min(512, std::max(32, (1 << n) / 2));
+    if (kmax <= 2)
+        k_small_run<2><<<1, threads, smem, s->stream>>>((double2*)s->state, n, d_tg, (int)tg.size(), d_m, d_p, dprobs);
+    else
+        k_small_run<4><<<1, threads, smem, s->stream>>>((double2*)s->state, n, d_tg, (int)tg.size(), d_m, d_p, dprobs);
+    s->stats.kernel_launches++;
+    s->stats.sweeps++;
+    s->stats.gates += (int64_t)tg.size();
+    s->stats.bytes_moved += 16.0 * (double)((int64_t)1 << n);
+    return bs_cuda_check(s, cudaGetLastError(), "small run");
 }

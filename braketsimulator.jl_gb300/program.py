@@ -311,9 +311,15 @@ def simulate(sim, program: Program, shots: int = 0, seed: int | None = None, mma
     ops = list(program.instructions)
     if shots > 0 and program.basis_rotation_instructions:
         ops += list(program.basis_rotation_instructions)
-    sim.reinit(n, shots)
-    sim.evolve(ops)
     measured = sorted(_measured_qubits(program, n))
+    small = isinstance(sim, StateVectorSimulator) and n <= 12 and shots > 0 and mmap_threshold is None
+    if small:
+        # reinit!, evolve! and the shots in one round trip (bs_run_small)
+        sim.reinit(n, shots)
+        _, s = sim.run(ops, shots, seed, probabilities=False)
+    else:
+        sim.reinit(n, shots)
+        sim.evolve(ops)
     results, paths, lens = [], (), ()
     if shots == 0 and program.results:
         if mmap_threshold is None:
@@ -322,7 +328,8 @@ def simulate(sim, program: Program, shots: int = 0, seed: int | None = None, mma
             results, paths, lens = _mmap_results(sim, program, n, int(mmap_threshold), mmap_dir)
     measurements = None
     if shots > 0:
-        s = sim.samples(seed)
+        if not small:
+            s = sim.samples(seed)
         bits = ((s[:, None] >> np.arange(n - 1, -1, -1)[None, :]) & 1).astype(np.int64)
         measurements = bits[:, measured]
     out = {"measurements": measurements, "resultTypes": results, "measuredQubits": measured,

@@ -49,7 +49,8 @@ class Sample:
 
 
 def marginal_probability(probs: np.ndarray, qubit_count: int, targets) -> np.ndarray:
-    """src/result_types.jl:96-113 on a host vector: output bit j <-> j-th smallest endian target."""
+    """src/result_types.jl:96-113 on a host vector a caller holds: output bit j <-> j-th smallest
+    endian target.  Simulators compute marginals on the device (``marginal_probabilities``)."""
     targets = list(targets)
     p = np.asarray(probs, dtype=np.float64).reshape([2] * qubit_count) if qubit_count else np.asarray(probs)
     unused = [q for q in range(qubit_count) if q not in targets]
@@ -109,8 +110,9 @@ def _swap_bits(ix, mapping):
 
 
 def partial_trace(state, output_qubits=None):
-    """Reduced density matrix (src/sv_simulator.jl:273-318 for a vector,
-    src/dm_simulator.jl:280-323 for a matrix)."""
+    """Reduced density matrix of a host array (src/sv_simulator.jl:273-318 for a vector,
+    src/dm_simulator.jl:280-323 for a matrix), the reference's loops restated for arrays a caller
+    holds; simulators compute the same on the device (``reduced_density_matrix``)."""
     state = np.asarray(state, dtype=np.complex128)
     vec = state.ndim == 1
     n = int(round(np.log2(state.shape[0])))
@@ -214,9 +216,7 @@ def calculate(rt, sim):
             return sim.probabilities()
         if len(t) == n:
             return permute_probability(sim.probabilities(), n, list(t))
-        if len(t) <= 12:
-            return sim.marginal_probabilities(sorted(t))
-        return marginal_probability(sim.probabilities(), n, t)
+        return sim.marginal_probabilities(sorted(t))
     if isinstance(rt, Expectation):
         t = _targets(rt, sim)
         if len(t) == rt.observable.qubit_count():
@@ -235,7 +235,5 @@ def calculate(rt, sim):
             return rho if full else sim.density_matrix()
         if len(t) == n:
             return permute_density_matrix(rho if full else sim.density_matrix(), n, list(t))
-        if 1 <= len(set(t)) <= 12 and len(set(t)) < n:
-            return reduced_density_matrix(sim, list(t))
-        return partial_trace(rho if full else sim.state_vector, list(t))
+        return reduced_density_matrix(sim, list(t))
     raise TypeError(f"unsupported result type {rt!r}")

@@ -267,10 +267,12 @@ class AbstractSimulator:
         return out
 
     def samples_from_stream(self, j: np.ndarray, u: np.ndarray, wsum: float | None = None,
-                            probabilities: np.ndarray | None = None) -> np.ndarray:
+                            probabilities: np.ndarray | None = None, parallel: bool = False) -> np.ndarray:
         """Alias-table draws on a supplied stream: j plays rand(rng, 1:N) - 1, u plays rand(rng).
         With ``probabilities`` the table is built from that vector (bit-exact with the reference's
-        make_alias_table! given the same wsum); otherwise from the simulator's state."""
+        make_alias_table! given the same wsum); otherwise from the simulator's state, serially in the
+        reference's order or, with ``parallel``, by the parallel construction (same distribution,
+        another table)."""
         j = np.ascontiguousarray(j, dtype=np.int64)
         u = np.ascontiguousarray(u, dtype=np.float64)
         if probabilities is not None:
@@ -278,10 +280,16 @@ class AbstractSimulator:
             ws = float(np.sum(p)) if wsum is None else float(wsum)
             self._h.call("bs_alias_build_from", _abi.dptr(p), p.size, ws)
         else:
-            self._h.call("bs_alias_build", -1.0 if wsum is None else float(wsum), 0)
+            self.alias_build(wsum, parallel)
         out = np.empty(j.size, dtype=np.int64)
         self._h.call("bs_sample_alias", _abi.i64ptr(j), _abi.dptr(u), j.size, _abi.i64ptr(out))
         return out
+
+    def alias_build(self, wsum: float | None = None, parallel: bool = False):
+        """Alias table of the current probabilities on the device (make_alias_table!,
+        src/result_types.jl:8-54): serial in the reference's order, or the parallel construction."""
+        flags = _abi.BS_ALIAS_PARALLEL if parallel else _abi.BS_ALIAS_EXACT
+        self._h.call("bs_alias_build", -1.0 if wsum is None else float(wsum), flags)
 
     def alias_table(self):
         n = 1 << self.qubit_count
@@ -298,7 +306,7 @@ class AbstractSimulator:
         return out
 
     def reduced_density_matrix(self, qubits) -> np.ndarray:
-        """Partial trace keeping ``qubits`` (1..12 of them), on the device; row/column index bit r
+        """Partial trace keeping ``qubits`` (1..16 of them), on the device; row/column index bit r
         belongs to the r-th highest-numbered kept qubit (the reference's loop order)."""
         q = np.ascontiguousarray(list(qubits), dtype=np.int32)
         d = 1 << q.size
@@ -338,9 +346,28 @@ class StateVectorSimulator(AbstractSimulator):
     def state_vector(self, v):
         self._set(v)
 
+    def run(self, instructions: Sequence[Instruction], shots: int | None = None, seed: int | None = None,
+            probabilities: bool = True):
+        """simulate of one circuit from |0...0> (src/BraketSimulator.jl:307-322: reinit!, evolve!, then
+        probabilities and samples) in one round trip to the GPU for states of at most 12 qubits:
+        returns (probabilities or None, samples).  The samples are those ``samples(seed)`` draws after
+        ``reinit`` and ``evolve``; the simulator keeps the final state."""
+        shots = self.shots if shots is None else int(shots)
+        if seed is None:
+            self.seed += 1
+            seed = self.seed
+        arr, n_ops, keep = _ops_for(instructions, False, 0)
+        p = np.empty(1 << self.qubit_count, dtype=np.float64) if probabilities else None
+        smp = np.empty(shots, dtype=np.int64)
+        self._h.call("bs_run_small", arr, n_ops, shots, C.c_uint64(seed & 0xFFFFFFFFFFFFFFFF),
+                     _abi.dptr(p) if p is not None else None, _abi.i64ptr(smp))
+        del keep
+        self._obs = None
+        return p, smp
+
     def density_matrix(self) -> np.ndarray:
-        v = self._get()
-        return np.outer(v, v.conj())
+        """psi psi^dagger (src/sv_simulator.jl:151-152), formed on the device (at most 16 qubits)."""
+        return self.reduced_density_matrix(range(self.qubit_count))
 
     def _state_value(self):
         return self._get()

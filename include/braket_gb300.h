@@ -129,6 +129,15 @@ int bs_apply_kraus(bs_sim* sim, const double* kraus, int n_kraus, int n_targets,
 int bs_evolve(bs_sim* sim, const bs_op* ops, int64_t n_ops, unsigned noise_mode);
 int bs_last_stats(const bs_sim* sim, bs_stats* out);
 
+/* ---- simulate of one small circuit (src/BraketSimulator.jl:307-322: reinit!, evolve!, then the
+ *      results) in one round trip: the state is reset to |0...0>, the ops are applied, and
+ *      probs_out (2^n doubles, may be null) and samples_out (shots basis indices, bs_sample's
+ *      generator with this seed) are filled.  The handle keeps the final state, as after
+ *      bs_reinit + bs_evolve.  State vectors of at most 12 qubits (complex128 runs in one CTA; other
+ *      cases take the usual kernels with the same results). */
+int bs_run_small(bs_sim* sim, const bs_op* ops, int64_t n_ops, int64_t shots, uint64_t seed, double* probs_out,
+                 int64_t* samples_out);
+
 /* ---- probabilities (src/sv_simulator.jl:271, src/dm_simulator.jl:262) */
 int bs_probabilities(bs_sim* sim, double* host_out, int64_t n);
 /* marginal_probability (src/result_types.jl:96-113): sum over the qubits not in targets,

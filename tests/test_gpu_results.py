@@ -1,4 +1,6 @@
 """Probabilities, expectations, variances, marginals and sampling on the GPU."""
+import math
+
 import numpy as np
 import pytest
 
@@ -152,6 +154,76 @@ def test_alias_bit_exact_on_supplied_stream(n):
     assert np.array_equal(got, oracle.sample_alias(ap, al, j, u))
 
 
+def _represented(ap, al):
+    """Distribution an alias table encodes (times n): bucket b keeps ap[b] for itself and gives
+    1 - ap[b] to alias[b]."""
+    w = np.array(ap, dtype=np.float64)
+    give = np.where(al >= 0, 1.0 - ap, 0.0)
+    np.add.at(w, np.where(al >= 0, al, 0), give)
+    return w
+
+
+@pytest.mark.parametrize("n,kind", [(1, "sv"), (6, "sv"), (12, "sv"), (20, "sv"), (6, "dm"), (16, "c64")])
+def test_parallel_alias_table_is_valid_and_exact(n, kind):
+    """BS_ALIAS_PARALLEL: a different table from the reference's serial one, for the same
+    distribution.  Every bucket is a probability with a valid alias where it is below 1, and the
+    distribution the table encodes equals the state's probabilities to rounding."""
+    rng = np.random.default_rng(40 + n)
+    if kind == "dm":
+        sim = bs.DensityMatrixSimulator(n, 0).evolve(random_circuit(n, 20, rng))
+    else:
+        sim = bs.StateVectorSimulator(n, 0, precision="c64" if kind == "c64" else "c128")
+        sim.evolve(random_circuit(n, 40, rng))
+    p = sim.probabilities()
+    N = p.size
+    sim.alias_build(parallel=True)
+    ap, al = sim.alias_table()
+    assert np.all((ap >= 0) & (ap <= 1))
+    low = ap < 1
+    assert np.all((al[low] >= 0) & (al[low] < N) & (al[low] != np.arange(N)[low]))
+    target = p * N / math.fsum(p)
+    # the weights' own FP64 roundings leave at most ~2.2e-16 N of weight unbalanced (it stays with the
+    # last bucket, as the serial algorithm's leftovers do); everything else is exact
+    scale = max(1.0, float(np.max(target)))
+    assert np.max(np.abs(_represented(ap, al) - target)) < 3e-16 * N + 1e-12 * scale
+    # the serial table (float-float weight sum) encodes the same distribution
+    sim.alias_build(parallel=False)
+    sap, sal = sim.alias_table()
+    assert np.max(np.abs(_represented(sap, sal) - target)) < 4e-15 * N + 1e-10 * scale
+
+
+def test_parallel_alias_extreme_distributions():
+    """One populated basis state; all weight equal; one state holding half of it."""
+    for prep in ([bs.Instruction(bs.X(), [3])], [bs.Instruction(bs.H(), [q]) for q in range(8)],
+                 [bs.Instruction(bs.H(), [0]), bs.Instruction(bs.CNot(), [0, 5])] +
+                 [bs.Instruction(bs.Ry(0.3 * (q + 1)), [q]) for q in range(1, 5)]):
+        sim = bs.StateVectorSimulator(8, 0).evolve(prep)
+        p = sim.probabilities()
+        sim.alias_build(parallel=True)
+        ap, al = sim.alias_table()
+        assert np.all((ap >= 0) & (ap <= 1))
+        assert np.all(al[ap < 1] >= 0)
+        assert np.max(np.abs(_represented(ap, al) - p * 256 / math.fsum(p))) < 1e-12 * 256
+
+
+def test_parallel_alias_draws_follow_the_distribution():
+    n, shots = 10, 400000
+    rng = np.random.default_rng(5)
+    sim = bs.StateVectorSimulator(n, 0).evolve(random_circuit(n, 40, rng))
+    p = sim.probabilities()
+    j = rng.integers(0, 2 ** n, shots)
+    u = rng.random(shots)
+    got = sim.samples_from_stream(j, u, parallel=True)
+    ap, al = sim.alias_table()
+    assert np.array_equal(got, oracle.sample_alias(ap, al, j, u))     # the draw rule on the same table
+    counts = np.bincount(got, minlength=2 ** n)
+    exp = p / p.sum() * shots
+    keep = exp > 20
+    chi2 = float(np.sum((counts[keep] - exp[keep]) ** 2 / exp[keep]))
+    dof = int(keep.sum()) - 1
+    assert chi2 < dof + 6 * np.sqrt(2 * dof)
+
+
 @pytest.mark.parametrize("n", [6, 12, 18])
 def test_direct_sampling_matches_linear_scan(n):
     rng = np.random.default_rng(n + 1)
@@ -216,6 +288,60 @@ def test_device_partial_trace_matches_host(n, keep):
         dm.evolve(ops + [bs.Instruction(bs.Depolarizing(0.1), [0])])
         rho = dm.density_matrix
         assert np.max(np.abs(bs.calculate(bs.DensityMatrix(keep), dm) - bs.partial_trace(rho, list(keep)))) < 1e-13
+
+
+@pytest.mark.parametrize("n,keep", [(17, tuple(range(1, 15))), (15, tuple(range(15))), (16, tuple(range(0, 16, 1))[2:])])
+def test_device_partial_trace_wide(n, keep):
+    """More than 12 kept qubits (and all of them: the state vector's density matrix) on the device,
+    against the same matrix by tensor contraction of the oracle's state."""
+    rng = np.random.default_rng(n + 3 * len(keep))
+    ops = random_circuit(n, 30, rng)
+    sv = bs.StateVectorSimulator(n, 0).evolve(ops)
+    got = bs.calculate(bs.DensityMatrix(keep), sv)
+    psi = oracle.OracleSV(n).evolve(ops).psi
+    kept = sorted(keep)
+    tr = [q for q in range(n) if q not in kept]
+    a = np.transpose(psi.reshape([2] * n), kept + tr).reshape(1 << len(kept), -1)
+    ref = a @ a.conj().T
+    assert rel_err(got, ref) < 1e-12
+
+
+def test_state_vector_density_matrix_on_device():
+    n = 11
+    ops = random_circuit(n, 40, np.random.default_rng(8))
+    sv = bs.StateVectorSimulator(n, 0).evolve(ops)
+    psi = oracle.OracleSV(n).evolve(ops).psi
+    assert rel_err(sv.density_matrix(), np.outer(psi, psi.conj())) < 1e-12
+    assert rel_err(bs.calculate(bs.DensityMatrix(()), sv), np.outer(psi, psi.conj())) < 1e-12
+
+
+def test_density_matrix_keep_all_13_qubits_on_device():
+    n = 13
+    dm = bs.DensityMatrixSimulator(n, 0)
+    dm.evolve([bs.Instruction(bs.H(), [q]) for q in range(n)] + [bs.Instruction(bs.CNot(), [0, 12]),
+              bs.Instruction(bs.Depolarizing(0.2), [5]), bs.Instruction(bs.Ry(0.7), [12])])
+    assert rel_err(dm.reduced_density_matrix(range(n)), dm.density_matrix) < 1e-13
+
+
+@pytest.mark.parametrize("kind,n,k,precision", [("sv", 18, 13, "c128"), ("sv", 18, 16, "c128"), ("sv", 17, 17, "c128"),
+                                                ("sv", 18, 14, "c64"), ("dm", 13, 13, "c128")])
+def test_marginal_probabilities_wide(kind, n, k, precision):
+    """Marginals over more than 12 targets on the device (no host fallback) against the oracle's
+    probabilities summed over the other qubits."""
+    rng = np.random.default_rng(n * 7 + k)
+    ops = random_circuit(n, 30 if kind == "sv" else 12, rng)
+    if kind == "sv":
+        sim = bs.StateVectorSimulator(n, 0, precision=precision).evolve(ops)
+        p = np.abs(oracle.OracleSV(n).evolve(ops).psi) ** 2
+    else:
+        sim = bs.DensityMatrixSimulator(n, 0).evolve(ops)
+        p = oracle.OracleDM(n).evolve(ops).probabilities()
+    targets = sorted(int(x) for x in rng.choice(n, k, replace=False))
+    got = bs.calculate(bs.Probability(tuple(targets)), sim) if k < n else sim.marginal_probabilities(targets)
+    traced = tuple(q for q in range(n) if q not in targets)
+    ref = p.reshape([2] * n).sum(axis=traced).reshape(-1) if traced else p
+    tol = 1e-12 if precision == "c128" else 1e-6
+    assert np.max(np.abs(got - ref)) < tol * max(1.0, float(np.max(ref)))
 
 
 def test_device_partial_trace_complex64():
