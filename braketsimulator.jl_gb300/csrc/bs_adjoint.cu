@@ -394,6 +394,194 @@ __global__ void __launch_bounds__(kAThreads) k_adjoint_sweep(typename Elem<C64>:
     }
 }
 
+// ---- complex64 states: the backward sweep's gates in FP32 on float2 tiles (the state's own
+// precision; half the shared memory and a sixth of the instructions of the float-float path), the
+// gradient inner products from the FP32 values with exact products and float-float sums.
+__device__ __forceinline__ float2 c32mul(float2 m, float2 x) {
+    return make_float2(__fmaf_rn(m.x, x.x, -m.y * x.y), __fmaf_rn(m.x, x.y, m.y * x.x));
+}
+__device__ __forceinline__ float2 c32ipow(float2 x, int p) {
+    switch (p & 3) {
+        case 0: return x;
+        case 1: return make_float2(-x.y, x.x);
+        case 2: return make_float2(-x.x, -x.y);
+        default: return make_float2(x.y, -x.x);
+    }
+}
+// matrix entry (float4 re hi, re lo, im hi, im lo) as the nearest complex64 value
+__device__ __forceinline__ float2 m32(float4 v) { return make_float2(v.x, v.z); }
+
+template <int K>
+__device__ void adj32_dense2(float2* sa, float2* sb, int T, const TileGate& g, const float4* __restrict__ mats) {
+    constexpr int D = 1 << K;
+    int pos[K];
+    for (int q = 0; q < K; q++) pos[q] = g.tbit[q];
+    for (int a = 0; a < K; a++)
+        for (int b = a + 1; b < K; b++)
+            if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
+    const float4* m = mats + g.mat_off;
+    for (int gr = threadIdx.x; gr < (1 << (T - K)); gr += blockDim.x) {
+        int jb = gr;
+        for (int q = 0; q < K; q++) { int low = jb & ((1 << pos[q]) - 1); jb = ((jb >> pos[q]) << (pos[q] + 1)) | low; }
+        if ((jb & (int)g.lc_mask) != (int)g.lc_val) continue;
+        float2 x[D], y[D];
+        int idx[D];
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+            int j = jb;
+            for (int q = 0; q < K; q++) if ((c >> q) & 1) j |= 1 << g.tbit[q];
+            idx[c] = j;
+            x[c] = sa[j];
+            y[c] = sb[j];
+        }
+#pragma unroll
+        for (int r = 0; r < D; r++) {
+            float2 u = make_float2(0.f, 0.f), v = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int c = 0; c < D; c++) {
+                const float2 mc = m32(__ldg(m + r * D + c));
+                u.x = __fmaf_rn(mc.x, x[c].x, __fmaf_rn(-mc.y, x[c].y, u.x));
+                u.y = __fmaf_rn(mc.x, x[c].y, __fmaf_rn(mc.y, x[c].x, u.y));
+                v.x = __fmaf_rn(mc.x, y[c].x, __fmaf_rn(-mc.y, y[c].y, v.x));
+                v.y = __fmaf_rn(mc.x, y[c].y, __fmaf_rn(mc.y, y[c].x, v.y));
+            }
+            sa[idx[r]] = u;
+            sb[idx[r]] = v;
+        }
+    }
+}
+
+__device__ void adj32_apply2(float2* sa, float2* sb, int T, int L, const TileGate& g, const float4* mats,
+                             const int32_t* perms, int64_t base, const int64_t* off_tab) {
+    const int nt = 1 << T, lowmask = (1 << L) - 1;
+    if (g.kind == 1) {
+        const float4* m = mats + g.mat_off;
+        for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+            if ((j & (int)g.lc_mask) != (int)g.lc_val) continue;
+            const int64_t gi = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+            int di = 0;
+            for (int q = 0; q < g.k; q++) di |= (int)((gi >> g.gbit[q]) & 1) << q;
+            const float2 d = m32(__ldg(m + di));
+            sa[j] = c32mul(d, sa[j]);
+            sb[j] = c32mul(d, sb[j]);
+        }
+    } else if (g.kind == 0) {
+        switch (g.k) {
+            case 1: adj32_dense2<1>(sa, sb, T, g, mats); break;
+            case 2: adj32_dense2<2>(sa, sb, T, g, mats); break;
+            case 3: adj32_dense2<3>(sa, sb, T, g, mats); break;
+            default: adj32_dense2<4>(sa, sb, T, g, mats); break;
+        }
+    } else {
+        // monomial: column c goes to row perm[2c] with phase i^perm[2c+1]
+        const int D = 1 << g.k;
+        int pos[BS_TILE_MAXK];
+        for (int q = 0; q < g.k; q++) pos[q] = g.tbit[q];
+        for (int a = 0; a < g.k; a++)
+            for (int b = a + 1; b < g.k; b++)
+                if (pos[b] < pos[a]) { int t = pos[a]; pos[a] = pos[b]; pos[b] = t; }
+        const int32_t* p = perms + g.perm_off;
+        for (int gr = threadIdx.x; gr < (1 << (T - g.k)); gr += blockDim.x) {
+            int jb = gr;
+            for (int q = 0; q < g.k; q++) { int low = jb & ((1 << pos[q]) - 1); jb = ((jb >> pos[q]) << (pos[q] + 1)) | low; }
+            if ((jb & (int)g.lc_mask) != (int)g.lc_val) continue;
+            float2 x[16], y[16];
+            int idx[16];
+            for (int c = 0; c < D; c++) {
+                int j = jb;
+                for (int q = 0; q < g.k; q++) if ((c >> q) & 1) j |= 1 << g.tbit[q];
+                idx[c] = j;
+                x[c] = sa[j];
+                y[c] = sb[j];
+            }
+            for (int c = 0; c < D; c++) {
+                const int r = __ldg(p + 2 * c), ph = __ldg(p + 2 * c + 1);
+                sa[idx[r]] = c32ipow(x[c], ph);
+                sb[idx[r]] = c32ipow(y[c], ph);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kAThreads) k_adjoint_sweep_c64(float2* __restrict__ psi, float2* __restrict__ lam,
+                                                                 SweepDesc d, const AdjGate* __restrict__ ag,
+                                                                 double* __restrict__ grad_acc, int64_t tile0) {
+    extern __shared__ float4 smem4[];
+    const int T = d.T, L = d.L, H = T - L;
+    const int nt = 1 << T;
+    float2* sp = reinterpret_cast<float2*>(smem4);
+    float2* sl = sp + nt;
+    int64_t* off_tab = reinterpret_cast<int64_t*>(sl + nt);
+    __shared__ int64_t s_base;
+    __shared__ double red[kAThreads / 32];
+    const int64_t tile = tile0 + (int64_t)blockIdx.x;
+    if (threadIdx.x == 0) {
+        int64_t base = 0;
+        int src = 0;
+        for (int bit = 0; bit < d.n_bits; bit++)
+            if (!((d.tile_mask >> bit) & 1ULL)) { base |= ((tile >> src) & 1LL) << bit; src++; }
+        s_base = base;
+    }
+    for (int i = threadIdx.x; i < (1 << H); i += blockDim.x) {
+        int64_t o = 0;
+        for (int j = 0; j < H; j++) if ((i >> j) & 1) o |= 1LL << d.hi_bits[j];
+        off_tab[i] = o;
+    }
+    __syncthreads();
+    const int64_t base = s_base;
+    const int lowmask = (1 << L) - 1;
+#pragma unroll 4
+    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        const int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+        sp[j] = psi[gidx];
+        sl[j] = lam[gidx];
+    }
+    __syncthreads();
+    for (int gi = 0; gi < d.n_gates; gi++) {
+        const AdjGate& a = ag[gi];
+        if (a.g.kind == 3) {
+            // Im <lambda| G |psi> over the tile: exact FP32 products, float-float sums
+            ffsum acc{0.f, 0.f};
+            for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+                const int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+                const float2 l = sl[j];
+                float2 x;
+                if (a.projector) {
+                    if (!((gidx >> a.g.gbit[0]) & 1)) continue;
+                    x = sp[j];
+                } else {
+                    const int ph = a.ph + ((__popcll((unsigned long long)gidx & a.zm) & 1) ? 2 : 0);
+                    x = c32ipow(sp[j ^ (int)a.xm_local], (4 - (ph & 3)) & 3);
+                }
+                ffacc m;
+                acc_first(m, l.x, 0.f, x.y, 0.f);
+                acc_add(m, -l.y, 0.f, x.x, 0.f);
+                const ff v = acc_done(m);
+                fsum_add(acc, v.h, v.l);
+            }
+            double v = ff2d(acc.h, acc.l) * a.weight;
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double t = 0.0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+                atomicAdd(grad_acc + a.slot, t);
+            }
+            __syncthreads();
+            continue;
+        }
+        if ((base & (int64_t)a.g.gc_mask) != (int64_t)a.g.gc_val) continue;
+        adj32_apply2(sp, sl, T, L, a.g, d.mats, d.perms, base, off_tab);
+        __syncthreads();
+    }
+    for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        const int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
+        psi[gidx] = sp[j];
+        lam[gidx] = sl[j];
+    }
+}
+
 inline float4 to_cff(double re, double im) {
     float4 v;
     v.x = (float)re; v.y = (float)(re - (double)v.x);
@@ -727,7 +915,8 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
     const int H = T - L;
     const size_t smem = (size_t)2 * ((size_t)1 << T) * sizeof(float4) + ((size_t)1 << H) * sizeof(int64_t);
     cudaFuncSetAttribute(k_adjoint_sweep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_adjoint_sweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_adjoint_sweep_c64, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    const size_t smem64 = (size_t)2 * ((size_t)1 << T) * sizeof(float2) + ((size_t)1 << H) * sizeof(int64_t);
     const int64_t ntiles = (int64_t)1 << (n_bits - T);
     for (size_t sw = 0; sw < sweeps_items.size(); sw++) {
         if (sweep_restore[sw] >= 0)
@@ -745,8 +934,8 @@ extern "C" int bs_adjoint_gradient(bs_sim* s, const bs_op* ops, int64_t n_ops, c
         for (int64_t t0 = 0; t0 < ntiles; t0 += (1LL << 30)) {
             int64_t nb = std::min<int64_t>(ntiles - t0, 1LL << 30);
             if (c64)
-                k_adjoint_sweep<true><<<(unsigned)nb, kAThreads, smem, s->stream>>>((float2*)s->state, (float2*)lam, d,
-                                                                                     d_ag + sweep_first[sw], d_acc, t0);
+                k_adjoint_sweep_c64<<<(unsigned)nb, kAThreads, smem64, s->stream>>>((float2*)s->state, (float2*)lam, d,
+                                                                                    d_ag + sweep_first[sw], d_acc, t0);
             else
                 k_adjoint_sweep<false><<<(unsigned)nb, kAThreads, smem, s->stream>>>((double2*)s->state, (double2*)lam, d,
                                                                                       d_ag + sweep_first[sw], d_acc, t0);

@@ -397,10 +397,10 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
 // fused gate), so one CTA's MMAs overlap the other's CUDA-core work.  The tile is stored with the
 // bank swizzle tc::sw.
 #ifndef BS_TC_THREADS
-#define BS_TC_THREADS 256
+#define BS_TC_THREADS 512
 #endif
-constexpr int kTcThreads = BS_TC_THREADS;   // 256 (128 registers) or 512 (64 registers, spills; measured slower)
-constexpr int kTcSmem = 49152 + 65536;
+constexpr int kTcThreads = BS_TC_THREADS;   // one CTA of 16 warps per SM (128 registers each)
+constexpr int kTcSmem = 2 * 49152 + 65536;   // two digit-slice buffers and the tile: one CTA per SM
 
 // Global offset (>> 5) of the tile's high-bit pattern i (7 bits) from two small tables:
 // a[i & 7] | b[i >> 3].
@@ -410,13 +410,13 @@ struct HiOff {
     __device__ __forceinline__ uint32_t operator[](int i) const { return a[i & 7] | b[i >> 3]; }
 };
 
-__global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __restrict__ psi, SweepDesc d, int64_t tile0,
+__global__ void __launch_bounds__(kTcThreads, 1) k_tile_sweep_tc(double2* __restrict__ psi, SweepDesc d, int64_t tile0,
                                                                  int tc_last) {
     // 128-byte alignment: each 128-byte core matrix of the matrix operand sits in one shared-memory line
     extern __shared__ __align__(128) unsigned char dsm[];
-    uint16_t* sB = reinterpret_cast<uint16_t*>(dsm);
-    float4* smem = reinterpret_cast<float4*>(dsm + 49152);
-    __shared__ __align__(8) uint64_t bars[7];   // digit copy, MMAs into D0 / D1, D0 / D1 read, D1 free, D2
+    uint16_t* sB = reinterpret_cast<uint16_t*>(dsm);                 // two 48 KiB digit-slice buffers
+    float4* smem = reinterpret_cast<float4*>(dsm + 2 * 49152);
+    __shared__ __align__(8) uint64_t bars[7];   // digit copies into buffers 0 / 1, MMAs of rounds 0..4 done
     __shared__ uint32_t s_tmem;
     __shared__ int64_t s_base;
     __shared__ int s_fail;
@@ -425,7 +425,6 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
     __shared__ uint32_t s_wmax[kTcThreads / 32];   // per-warp largest high-word exponent field
     __shared__ int s_act[32], s_cnt;                 // kind 5: blocks passing the row/column test
     __shared__ int s_tcq[16], s_ntc;                 // the tile's first 16 fused gates, in order
-    __shared__ const uint16_t* s_nsrc;
     const HiOff off32{s_offa, s_offb};
     constexpr int T = 12, L = 5, H = 7, nt = 1 << T, lowmask = (1 << L) - 1;
     const int64_t tile = tile0 + (int64_t)blockIdx.x;
@@ -436,13 +435,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
             if (!((d.tile_mask >> bit) & 1ULL)) { base |= ((tile >> src) & 1LL) << bit; src++; }
         s_base = base;
         s_fail = 0;
-        tc::mbar_init(tc::su32(&bars[0]));
-        tc::mbar_init(tc::su32(&bars[1]));
-        tc::mbar_init(tc::su32(&bars[2]));
-        tc::mbar_init_n(tc::su32(&bars[3]), kTcThreads / 32);
-        tc::mbar_init_n(tc::su32(&bars[4]), kTcThreads / 32);
-        tc::mbar_init(tc::su32(&bars[5]));
-        tc::mbar_init(tc::su32(&bars[6]));
+        for (int b = 0; b < 7; b++) tc::mbar_init(tc::su32(&bars[b]));
     }
     if (threadIdx.x < 24) {
         const int i = threadIdx.x < 8 ? threadIdx.x : (threadIdx.x - 8) << 3;
@@ -500,7 +493,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
         if ((threadIdx.x & 31) == 0) s_wmax[threadIdx.x >> 5] = eb;
     }
     __syncthreads();
-    tc::State st{0u, tc::su32(&bars[0]), 0u, s_ntc > 0};
+    tc::State st{0u, tc::su32(&bars[0]), 0u, s_ntc > 0 ? 1u : 0u, 0, s_ntc > 0, false};
     int q = 0;   // fused gates run so far
     bool have = false;
     bool emax_ok = true;   // s_wmax holds the tile's largest exponent (no magnitude-changing gate since)
@@ -520,8 +513,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
                 have = true;
             }
             const TileGate* gn = q + 1 < s_ntc ? d.gates + s_tcq[q + 1] : nullptr;
-            tc::apply<kTcThreads>(smem, g, gn, d.tc_pool, sB, st, base, s_wmax, emax_ok, s_tsw, &s_nsrc, &s_fail,
-                                  d.err);
+            tc::apply<kTcThreads>(smem, g, gn, d.tc_pool, sB, st, base, s_wmax, emax_ok, s_tsw, &s_fail, d.err);
             q++;
             emax_ok = true;
             if (gi == tc_last) {
@@ -556,10 +548,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
     if (have) {
         // a wait gave up: give the copies and MMAs in flight a bounded time to land before releasing TMEM
         if (threadIdx.x == 0 && s_fail) {
-            tc::mbar_wait(st.bar, st.ph & 1u);
-            tc::mbar_wait(st.bar + 8u, (st.ph >> 1) & 1u);
-            tc::mbar_wait(st.bar + 16u, (st.ph >> 2) & 1u);
-            tc::mbar_wait(st.bar + 48u, (st.ph >> 6) & 1u);
+            for (int b = 0; b < 2; b++)
+                if ((st.inflight >> b) & 1u) tc::mbar_wait(st.bar + 8u * (uint32_t)b, (st.ph >> b) & 1u);
+            if (st.mma_out) tc::mbar_wait(st.bar + 48u, (st.ph >> 6) & 1u);
         }
         __syncthreads();
         if (warp == 0) tc::tmem_dealloc(st.tmem);

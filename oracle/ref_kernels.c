@@ -266,34 +266,49 @@ void orc_dm_kraus_nq(cplx* rho, int64_t dim, const cplx* K, int nk, int k, const
 
 /* Physically complete channel (not in the reference): S' = sum_k conj(K) S K^T on the
  * stored matrix S, which is the convention the reference's gate path uses for S
- * (src/dm_simulator.jl:130-140).  Matrix index bit j <-> targets[j]. */
+ * (src/dm_simulator.jl:130-140).  Matrix index bit j <-> targets[j].  Written as the
+ * superoperator M[(r,c),(a,b)] = sum_q conj(K_q[r,a]) K_q[c,b] applied to every dk x dk
+ * block of S whose row and column share their non-target bits (blocks are disjoint, so the
+ * update is in place and parallel over blocks). */
+static inline int64_t dep_bits(int64_t x, const int* e, int k) {
+    int64_t g = 0;
+    for (int i = 0; i < k; i++) g |= ((x >> i) & 1) << e[i];
+    return g;
+}
 void orc_dm_kraus_full(cplx* rho, int64_t dim, const cplx* K, int nk, int k, const int* targets) {
     int nq = log2i(dim);
-    int64_t dk = (int64_t)1 << k;
-    int64_t mask = 0;
+    int64_t dk = (int64_t)1 << k, dk2 = dk * dk;
     int e[32];
-    for (int i = 0; i < k; i++) { e[i] = nq - 1 - targets[i]; mask |= (int64_t)1 << e[i]; }
-    cplx* out = (cplx*)calloc((size_t)(dim * dim), sizeof(cplx));
-    for (int64_t r = 0; r < dim; r++) for (int64_t c = 0; c < dim; c++) {
-        int64_t ri = 0, ci = 0;
-        for (int i = 0; i < k; i++) { ri |= ((r >> e[i]) & 1) << i; ci |= ((c >> e[i]) & 1) << i; }
-        cplx s = 0;
+    int sorted[32];
+    for (int i = 0; i < k; i++) { e[i] = nq - 1 - targets[i]; sorted[i] = e[i]; }
+    sort_ints(sorted, k);
+    cplx* M = (cplx*)malloc(sizeof(cplx) * (size_t)(dk2 * dk2));
+    for (int64_t r = 0; r < dk; r++) for (int64_t c = 0; c < dk; c++)
         for (int64_t a = 0; a < dk; a++) for (int64_t b = 0; b < dk; b++) {
-            int64_t rr = r & ~mask, cc = c & ~mask;
-            for (int i = 0; i < k; i++) { rr |= ((a >> i) & 1) << e[i]; cc |= ((b >> i) & 1) << e[i]; }
-            cplx v = rho[rr + cc * dim];
-            if (v == 0) continue;
             cplx w = 0;
             for (int q = 0; q < nk; q++) {
-                const cplx* Kq = K + (int64_t)q * dk * dk;
-                w += conj(Kq[ri * dk + a]) * Kq[ci * dk + b];
+                const cplx* Kq = K + (int64_t)q * dk2;
+                w += conj(Kq[r * dk + a]) * Kq[c * dk + b];
             }
-            s += w * v;
+            M[(r * dk + c) * dk2 + a * dk + b] = w;
         }
-        out[r + c * dim] = s;
+    const int64_t nb = dim >> k;   /* row (and column) bases */
+#pragma omp parallel for schedule(static) if (nb * nb >= 64)
+    for (int64_t ib = 0; ib < nb * nb; ib++) {
+        int64_t rb = pad_bits(ib % nb, sorted, k), cb = pad_bits(ib / nb, sorted, k);
+        cplx v[1024], o[1024];   /* dk <= 32 */
+        for (int64_t a = 0; a < dk; a++)
+            for (int64_t b = 0; b < dk; b++) v[a * dk + b] = rho[(rb | dep_bits(a, e, k)) + (cb | dep_bits(b, e, k)) * dim];
+        for (int64_t x = 0; x < dk2; x++) {
+            const cplx* Mx = M + x * dk2;
+            cplx s = 0;
+            for (int64_t y = 0; y < dk2; y++) s += Mx[y] * v[y];
+            o[x] = s;
+        }
+        for (int64_t r = 0; r < dk; r++)
+            for (int64_t c = 0; c < dk; c++) rho[(rb | dep_bits(r, e, k)) + (cb | dep_bits(c, e, k)) * dim] = o[r * dk + c];
     }
-    memcpy(rho, out, sizeof(cplx) * (size_t)(dim * dim));
-    free(out);
+    free(M);
 }
 
 /* ---------------- sampling ---------------- */
