@@ -38,15 +38,6 @@ struct PauliTerm {
 
 __device__ __forceinline__ cff f4c(float4 v) { return {v.x, v.y, v.z, v.w}; }
 __device__ __forceinline__ float4 c4f(const cff& c) { return make_float4(c.rh, c.rl, c.ih, c.il); }
-// the same layout as (high pair, low pair) for the packed arithmetic
-__device__ __forceinline__ void splitA(float4 v, f2& h, f2& l) {
-    h = pk(v.x, v.z);
-    l = pk(v.y, v.w);
-}
-__device__ __forceinline__ float4 joinA(f2 h, f2 l) {
-    const float2 a = up(h), b = up(l);
-    return make_float4(a.x, b.x, a.y, b.y);
-}
 
 // lambda_i = sum_t c_t (-i)^ph_t (-1)^popc(i & zm_t) psi_{i ^ xm_t}
 // C64: complex64 storage; the arithmetic and the sums stay float-float either way.
@@ -150,22 +141,11 @@ __device__ void adj_dense(float4* sm, int T, const TileGate& g, const float4* __
         }
 #pragma unroll
         for (int r = 0; r < D; r++) {
-            // packed complex float-float: the real and imaginary sums share a register pair
-            pacc y;
-            pcoef A, B;
-            f2 xh, xl;
-            splitA(c4f(x[0]), xh, xl);
-            pcoefs(__ldg(m + r * D), A, B);
-            pcmac_first(y, A, B, xh, xl, swap2(xh), swap2(xl));
+            ffacc ar, ai;
+            cmac_first(ar, ai, f4c(__ldg(m + r * D)), x[0]);
 #pragma unroll
-            for (int c = 1; c < D; c++) {
-                splitA(c4f(x[c]), xh, xl);
-                pcoefs(__ldg(m + r * D + c), A, B);
-                pcmac(y, A, B, xh, xl, swap2(xh), swap2(xl));
-            }
-            f2 yh, yl;
-            pacc_done(y, yh, yl);
-            sm[idx[r]] = joinA(yh, yl);
+            for (int c = 1; c < D; c++) cmac(ar, ai, f4c(__ldg(m + r * D + c)), x[c]);
+            sm[idx[r]] = c4f(cdone(ar, ai));
         }
     }
 }
@@ -232,35 +212,30 @@ __device__ void adj_dense2(float4* sa, float4* sb, int T, const TileGate& g, con
         int jb = gr;
         for (int q = 0; q < K; q++) { int low = jb & ((1 << pos[q]) - 1); jb = ((jb >> pos[q]) << (pos[q] + 1)) | low; }
         if ((jb & (int)g.lc_mask) != (int)g.lc_val) continue;
-        f2 xh[D], xl[D], yh[D], yl[D];
+        cff x[D], y[D];
         int idx[D];
 #pragma unroll
         for (int c = 0; c < D; c++) {
             int j = jb;
             for (int q = 0; q < K; q++) if ((c >> q) & 1) j |= 1 << g.tbit[q];
             idx[c] = j;
-            splitA(sa[j], xh[c], xl[c]);
-            splitA(sb[j], yh[c], yl[c]);
+            x[c] = f4c(sa[j]);
+            y[c] = f4c(sb[j]);
         }
 #pragma unroll
         for (int r = 0; r < D; r++) {
-            // packed complex float-float on both tiles, the matrix entry's coefficient pairs shared
-            pacc a, b;
-            pcoef A, B;
-            pcoefs(__ldg(m + r * D), A, B);
-            pcmac_first(a, A, B, xh[0], xl[0], swap2(xh[0]), swap2(xl[0]));
-            pcmac_first(b, A, B, yh[0], yl[0], swap2(yh[0]), swap2(yl[0]));
+            ffacc ar, ai, br, bi;
+            const cff m0 = f4c(__ldg(m + r * D));
+            cmac_first(ar, ai, m0, x[0]);
+            cmac_first(br, bi, m0, y[0]);
 #pragma unroll
             for (int c = 1; c < D; c++) {
-                pcoefs(__ldg(m + r * D + c), A, B);
-                pcmac(a, A, B, xh[c], xl[c], swap2(xh[c]), swap2(xl[c]));
-                pcmac(b, A, B, yh[c], yl[c], swap2(yh[c]), swap2(yl[c]));
+                const cff mc = f4c(__ldg(m + r * D + c));
+                cmac(ar, ai, mc, x[c]);
+                cmac(br, bi, mc, y[c]);
             }
-            f2 oh, ol;
-            pacc_done(a, oh, ol);
-            sa[idx[r]] = joinA(oh, ol);
-            pacc_done(b, oh, ol);
-            sb[idx[r]] = joinA(oh, ol);
+            sa[idx[r]] = c4f(cdone(ar, ai));
+            sb[idx[r]] = c4f(cdone(br, bi));
         }
     }
 }
@@ -275,15 +250,9 @@ __device__ void adj_apply2(float4* sa, float4* sb, int T, int L, const TileGate&
             const int64_t gi = base | off_tab[j >> L] | (int64_t)(j & lowmask);
             int di = 0;
             for (int q = 0; q < g.k; q++) di |= (int)((gi >> g.gbit[q]) & 1) << q;
-            pcoef A, B;
-            pcoefs(__ldg(m + di), A, B);
-            f2 xh, xl, oh, ol;
-            splitA(sa[j], xh, xl);
-            pcmul(A, B, xh, xl, oh, ol);
-            sa[j] = joinA(oh, ol);
-            splitA(sb[j], xh, xl);
-            pcmul(A, B, xh, xl, oh, ol);
-            sb[j] = joinA(oh, ol);
+            const cff dv = f4c(__ldg(m + di));
+            sa[j] = c4f(cmul(dv, f4c(sa[j])));
+            sb[j] = c4f(cmul(dv, f4c(sb[j])));
         }
     } else if (g.kind == 0 && g.k == 1) {
         adj_dense2<1>(sa, sb, T, g, mats);

@@ -199,81 +199,3 @@ __device__ __forceinline__ void fsum_add(ffsum& a, float xh, float xl) {
     a.h = __fadd_rn(t, lo);
     a.l = __fsub_rn(lo, __fsub_rn(a.h, t));
 }
-
-// ---------------------------------------------------------------- packed complex float-float
-// The same accumulation as ffacc, on register pairs: lane 0 carries the real part of a complex
-// sum and lane 1 its imaginary part, so that one packed instruction does the work of two and the
-// roundings of each lane are those of the scalar sequence.  A complex MAC m * x is two packed real
-// MACs: (mr, mr) * (xr, xi) + (-mi, mi) * (xi, xr).
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
-    f2 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-// (b, a) from (a, b)
-__device__ __forceinline__ f2 swap2(f2 v) { return (v >> 32) | (v << 32); }
-
-struct pacc { f2 s, c; };       // running sum (TwoSum-exact in s) and its error terms
-struct pcoef { f2 h, l, hn; };  // a packed coefficient: high words, low words, negated high words
-
-// coefficient pairs of a complex matrix entry (float4 re hi, re lo, im hi, im lo)
-__device__ __forceinline__ void pcoefs(float4 m, pcoef& a, pcoef& b) {
-    a.h = pk(m.x, m.x);
-    a.l = pk(m.y, m.y);
-    a.hn = pk(-m.x, -m.x);
-    b.h = pk(-m.z, m.z);
-    b.l = pk(-m.w, m.w);
-    b.hn = pk(m.z, -m.z);
-}
-// s + c = C * X exactly to ~2^-48 (TwoProd of the high words, cross terms in FP32)
-__device__ __forceinline__ void pacc_first(pacc& a, const pcoef& C, f2 xh, f2 xl) {
-    const f2 pn = mul2(C.hn, xh);
-    f2 e = fma2(C.h, xh, pn);
-    e = fma2(C.h, xl, e);
-    a.c = fma2(C.l, xh, e);
-    a.s = mul2(C.h, xh);
-}
-__device__ __forceinline__ void pacc_add(pacc& a, const pcoef& C, f2 xh, f2 xl) {
-    const f2 pn = mul2(C.hn, xh);              // -p
-    f2 e = fma2(C.h, xh, pn);                   // p's rounding error
-    e = fma2(C.h, xl, e);
-    e = fma2(C.l, xh, e);
-    const f2 t = sub2(a.s, pn);                 // TwoSum(s, p)
-    const f2 bb = sub2(t, a.s);
-    const f2 err = sub2(sub2(a.s, sub2(t, bb)), add2(pn, bb));
-    a.s = t;
-    a.c = add2(a.c, add2(e, err));
-}
-// complex MAC into one packed accumulator; xs = swap2 of the high and low pairs of x
-__device__ __forceinline__ void pcmac_first(pacc& a, const pcoef& A, const pcoef& B, f2 xh, f2 xl, f2 xsh, f2 xsl) {
-    pacc_first(a, A, xh, xl);
-    pacc_add(a, B, xsh, xsl);
-}
-__device__ __forceinline__ void pcmac(pacc& a, const pcoef& A, const pcoef& B, f2 xh, f2 xl, f2 xsh, f2 xsl) {
-    pacc_add(a, A, xh, xl);
-    pacc_add(a, B, xsh, xsl);
-}
-// normalised (high pair, low pair) of the sum
-__device__ __forceinline__ void pacc_done(const pacc& a, f2& h, f2& l) {
-    h = add2(a.s, a.c);
-    l = sub2(a.c, sub2(h, a.s));
-}
-// float4 (re hi, im hi, re lo, im lo) <-> high and low pairs
-__device__ __forceinline__ void split4(float4 v, f2& h, f2& l) {
-    h = pk(v.x, v.y);
-    l = pk(v.z, v.w);
-}
-__device__ __forceinline__ float4 join4(f2 h, f2 l) {
-    const float2 a = up(h), b = up(l);
-    return make_float4(a.x, a.y, b.x, b.y);
-}
-// coefficient pairs from the tile layout float4 (re hi, im hi, re lo, im lo)
-__device__ __forceinline__ void pcoefs_t(float4 m, pcoef& a, pcoef& b) {
-    pcoefs(make_float4(m.x, m.z, m.y, m.w), a, b);
-}
-// y = m * x for one complex value held as (high pair, low pair)
-__device__ __forceinline__ void pcmul(const pcoef& A, const pcoef& B, f2 xh, f2 xl, f2& yh, f2& yl) {
-    pacc y;
-    pcmac_first(y, A, B, xh, xl, swap2(xh), swap2(xl));
-    pacc_done(y, yh, yl);
-}

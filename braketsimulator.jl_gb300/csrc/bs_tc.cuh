@@ -35,8 +35,8 @@
 
 namespace tc {
 
-constexpr int kA0 = 0;          // first TMEM column of the six A digit slices
-constexpr uint32_t kCols = 512; // TMEM columns held by the one CTA of an SM
+constexpr int kA0 = 64;         // first TMEM column of the six A digit slices
+constexpr uint32_t kCols = 256; // TMEM columns held by one CTA
 // kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, N = 64, M = 128
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
 constexpr long long kSpin = 1LL << 31;   // cycles before a wait gives up (~1 s)
@@ -212,16 +212,15 @@ __device__ __forceinline__ f2 two_sum2(f2& s, f2 g) {
 
 struct State {
     uint32_t tmem;   // TMEM base address
-    uint32_t bar;    // seven mbarriers 8 bytes apart: 0, 1: digit-slice copy into buffer 0 / 1
-                     // (one arrival + bytes); 2..6: the MMAs of rounds 0..4 have completed (commits)
+    uint32_t bar;    // seven mbarriers 8 bytes apart: digit-slice copy (1 arrival + bytes), MMAs done into
+                     // D0, into D1 (commits), D0 read, D1 read (one arrival per warp), round 4's
+                     // state-digit-4/5 MMAs done, round 0 done into D2 (commits)
     uint32_t ph;     // expected phase parity of barrier k in bit k
-    uint32_t inflight;   // bit b: a copy into buffer b has been issued and not yet waited for
-    int buf;         // the digit-slice buffer of the gate about to run
-    bool pref;       // its slices were copied ahead (uniform)
-    bool mma_out;    // thread 0: MMAs issued whose last commit (barrier 6) nobody has waited for
+    bool pref;       // the digit slices of the gate about to run were copied ahead (uniform)
 };
 
-constexpr uint32_t kD = kA0 + 192;   // first accumulator column: round r at kD + 64 r (r = 0..4)
+constexpr uint32_t kD1 = kA0 + 128;   // second accumulator: the columns of A digit slices 4 and 5
+constexpr uint32_t kD2 = kA0 + 64;    // third accumulator (round 0 only): the columns of A digit slices 2 and 3
 
 // Source of a fused gate's digit slices for the CTA: the matrix variant selected by the base bits.
 __device__ __forceinline__ const uint16_t* slice_src(const TileGate& g, const uint16_t* pool, int64_t base) {
@@ -238,13 +237,14 @@ __device__ __forceinline__ void copy_slices(uint32_t sB, const uint16_t* src, ui
     bulk_g2s(sB, src, (uint32_t)kPoolBlock * 2, bar);
 }
 
-// One thread issues the MMAs of the digit pairs (i, j) with G0 <= i + j <= G1 (j: state digit,
-// i: matrix digit) into the accumulator at TMEM column dcol, the first one overwriting.  The pair set
-// is a compile-time constant so that the loops unroll and every operand address is the base plus a
-// constant: a single thread issues back to back (a run-time loop here doubled the time per MMA).
-// b0 = descriptor of the first digit slice; slice (i, s) starts (i*4+s)*2048 bytes later, which adds
-// (i*4+s)*128 to the 14-bit start-address field without carry (the slices span 48 KiB).
-template <int G0, int G1>
+// One thread issues the MMAs of the digit pairs (i, j) with G0 <= i + j <= G1 and JLO <= j <= JHI
+// (j: state digit, i: matrix digit) into the accumulator at TMEM column dcol; the first one
+// overwrites when OVERWRITE.  The pair set is a compile-time constant so that the loops unroll and
+// every operand address is the base plus a constant: a single thread issues back to back (a
+// run-time loop here doubled the time per MMA).  b0 = descriptor of the first digit slice; slice
+// (i, s) starts (i*4+s)*2048 bytes later, which adds (i*4+s)*128 to the 14-bit start-address field
+// without carry (the slices span 48 KiB).
+template <int G0, int G1, int JLO, int JHI, bool OVERWRITE>
 __device__ __forceinline__ void issue_pairs(uint32_t tmem, uint32_t dcol, uint64_t b0_) {
     // an opaque copy, so that the descriptors are formed here and not hoisted into registers
     // held across the caller's code
@@ -258,15 +258,21 @@ __device__ __forceinline__ void issue_pairs(uint32_t tmem, uint32_t dcol, uint64
 #pragma unroll
             for (int s = 0; s < 4; s++) {
                 const int i = gs - j;
-                if (i > 5 || j > 5) continue;
+                if (i > 5 || j > 5 || j < JLO || j > JHI) continue;
                 mma(tmem + dcol, tmem + (uint32_t)(kA0 + 32 * j + 8 * s), b0 + (uint64_t)((i * 4 + s) * 128),
-                    n == 0 ? 0u : 1u);
+                    (OVERWRITE && n == 0) ? 0u : 1u);
                 n++;
             }
 }
+// Round r < 4: the pairs of weight r, overwriting the accumulator, then a commit to bar.
+template <int ROUND>
+__device__ __forceinline__ void issue_round(uint32_t tmem, uint32_t dcol, uint64_t b0, uint32_t bar) {
+    issue_pairs<ROUND, ROUND, 0, 5, true>(tmem, dcol, b0);
+    commit(bar);
+}
 
 // Fold of one round's accumulator columns (this thread's NA amplitudes, re and im packed) into the
-// float-float sums: MODE 1: E += D, 2: S = D, 3: E += TwoSum(S, D) error with S updated.
+// float-float sums: MODE 0: E = D, 1: E += D, 2: S = D, 3: E += TwoSum(S, D) error with S updated.
 template <int MODE, int NA>
 __device__ __forceinline__ void fold(uint32_t taddr, f2 (&S)[NA], f2 (&E)[NA]) {
 #pragma unroll
@@ -281,7 +287,8 @@ __device__ __forceinline__ void fold(uint32_t taddr, f2 (&S)[NA], f2 (&E)[NA]) {
             for (int p = 0; p < 4; p++) {
                 const int o = 4 * (c2 + u) + p;
                 const f2 gv = pk(__uint_as_float(r[u][2 * p]), __uint_as_float(r[u][2 * p + 1]));
-                if (MODE == 1) E[o] = add2(E[o], gv);
+                if (MODE == 0) E[o] = gv;
+                else if (MODE == 1) E[o] = add2(E[o], gv);
                 else if (MODE == 2) S[o] = gv;
                 else E[o] = add2(E[o], two_sum2(S[o], gv));
             }
@@ -297,39 +304,32 @@ __device__ __forceinline__ bool wait_bar(State& st, int k, int lane_id) {
     fence_after();
     return done != 0;
 }
+// One thread's bounded wait (the parity flip is left to the caller, which flips it on every thread).
+__device__ __forceinline__ bool wait_bar1(const State& st, int k) {
+    const bool ok = mbar_wait(st.bar + 8u * (uint32_t)k, (st.ph >> k) & 1u);
+    fence_after();
+    return ok;
+}
 
 // Applies fused gate g to the (swizzled) 2^12 tile sm of float4 (re hi, im hi, re lo, im lo).
 // Called by all NT threads of the CTA (NT/128 threads per tile column, 32*128/NT amplitudes each),
-// which then synchronise.  sB0: two 48 KiB digit-slice buffers back to back; the gate uses buffer
-// st.buf, and gnext (the tile's next fused gate, or null) has its slices copied into the other one at
-// the start of this gate, so that copy overlaps this whole gate.  base: the CTA's global base index
-// (selects the matrix variant).  s_tsw: 32 ints of shared scratch; s_wmax: NT/32 per-warp maxima of
-// the high words' exponent fields.  The swizzle is linear over XOR, so the position of column m's
-// amplitude t is sw(column bits) ^ sw(target bits of t).
-// TMEM (512 columns, one CTA per SM): the six state-digit slices at kA0 + 32 j, the five round
-// accumulators at kD + 64 r.  Thread 0 issues all 104 MMAs in one go, round by round (0, 1, 2, 3, then
-// the 64 of weights 4..6), each round committed to its own barrier, so every warp folds a round as
-// soon as it completes while the tensor pipe runs the later ones.
+// which then synchronise.  base: the CTA's global base index (selects the matrix variant).  s_tsw:
+// 32 ints of shared scratch; s_wmax: NT/32 per-warp maxima of the high words' exponent fields.
+// gnext: the tile's next fused gate, whose digit slices are copied ahead as soon as this gate's
+// MMAs have completed (null: none, or it copies its own); s_nsrc: shared scratch for their source.
+// The swizzle is linear over XOR, so the position of column m's amplitude t is
+// sw(column bits) ^ sw(target bits of t).
 // On a wait that gives up, sets *fail and *err and leaves the tile partly updated.
 template <int NT>
 __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const TileGate* gnext,
-                                      const uint16_t* __restrict__ pool, uint16_t* sB0, State& st, int64_t base,
-                                      uint32_t* s_wmax, bool emax_ok, int* s_tsw, int* s_fail, int* err) {
+                                      const uint16_t* __restrict__ pool, uint16_t* sB, State& st, int64_t base,
+                                      uint32_t* s_wmax, bool emax_ok, int* s_tsw, const uint16_t** s_nsrc, int* s_fail,
+                                      int* err) {
     constexpr int HP = NT / 128;   // threads per column
     constexpr int NA = 32 / HP;    // amplitudes per thread
     const int tid = threadIdx.x, warp = tid >> 5, lane_id = tid & 31, m = tid & 127, h = tid >> 7;
-    const int buf = st.buf;
-    uint16_t* sB = sB0 + (size_t)buf * kPoolBlock;
-    if (tid == 0) {
-        // this gate's slices, unless copied ahead; the next gate's into the other buffer, whose last
-        // readers (the previous gate's MMAs) have completed
-        if (!st.pref) copy_slices(su32(sB), slice_src(g, pool, base), st.bar + 8u * (uint32_t)buf);
-        if (gnext)
-            copy_slices(su32(sB0 + (size_t)(buf ^ 1) * kPoolBlock), slice_src(*gnext, pool, base),
-                        st.bar + 8u * (uint32_t)(buf ^ 1));
-    }
-    st.inflight |= 1u << buf;
-    if (gnext) st.inflight |= 1u << (buf ^ 1);
+    // the previous readers of sB (the MMAs of the previous fused gate) have completed
+    if (!st.pref && tid == 0) copy_slices(su32(sB), slice_src(g, pool, base), st.bar);
     int tb[5];
     uint32_t tmask = 0;
 #pragma unroll
@@ -394,60 +394,80 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const TileG
     __syncthreads();
     fence_after();
     const uint64_t b0 = bdesc(su32(sB));
+    // Round 4 (weights 4..6, 64 MMAs) into D0 by thread 0: first the 20 MMAs that read state digits 4
+    // and 5, committed to barrier 5, so that D1, which takes their columns, is free once they have
+    // completed; thread 128 then issues round 3 into D1 while thread 0 still issues round 4.  Two
+    // issuers, each waiting only for the reads of its own accumulator: thread 0 runs D0 (rounds 4,
+    // 1), thread 128 runs D1 (rounds 3, 2) and round 0 into D2, the columns of state digits 2 and 3,
+    // which are free once rounds 4, 3 and 2 have completed.  Every warp folds the rounds in the order
+    // 4, 3, 2, 1, 0 (smallest digit weights first), E collecting rounds 4 and 3 in FP32 and S rounds
+    // 2, 1, 0 with their TwoSum errors into E.
     bool ok = true;
     if (tid == 0) {
-        if (mbar_wait(st.bar + 8u * (uint32_t)buf, (st.ph >> buf) & 1u)) {
+        if (mbar_wait(st.bar, st.ph & 1u)) {
             fence_after();
-            issue_pairs<0, 0>(st.tmem, kD, b0);
-            commit(st.bar + 16u);
-            issue_pairs<1, 1>(st.tmem, kD + 64u, b0);
-            commit(st.bar + 24u);
-            issue_pairs<2, 2>(st.tmem, kD + 128u, b0);
-            commit(st.bar + 32u);
-            issue_pairs<3, 3>(st.tmem, kD + 192u, b0);
+            issue_pairs<4, 6, 4, 5, true>(st.tmem, 0u, b0);
             commit(st.bar + 40u);
-            issue_pairs<4, 6>(st.tmem, kD + 256u, b0);
-            commit(st.bar + 48u);
-            st.mma_out = true;
+            issue_pairs<4, 6, 0, 3, false>(st.tmem, 0u, b0);
+            commit(st.bar + 8u);
         } else {
             ok = false;
         }
+    } else if (tid == 128) {
+        if (wait_bar1(st, 5)) issue_round<3>(st.tmem, kD1, b0, st.bar + 16u);
+        else ok = false;
+        if (gnext) *s_nsrc = slice_src(*gnext, pool, base);   // read back by this thread only
     }
-    // every thread moves past this copy's phase; thread 0, when its wait gave up, keeps it (and the copy
-    // in flight) so that the kernel's drain waits for that copy before releasing TMEM
-    if (ok) {
-        st.ph ^= 1u << buf;
-        st.inflight &= ~(1u << buf);
-    } else {
-        *s_fail = 1;
-        atomicExch(err, 1);
-    }
+    st.ph ^= 1u | (1u << 5);
+    if (!ok) { *s_fail = 1; atomicExch(err, 1); }
     f2 S[NA], E[NA];
-#pragma unroll
-    for (int a = 0; a < NA; a++) E[a] = 0ULL;
-    const uint32_t tl = st.tmem + lane + (uint32_t)(2 * NA * h) + kD;
-    // rounds 0, 1, 2 into S with their TwoSum errors into E, rounds 3 and 4 (small terms) into E
-    ok = wait_bar(st, 2, lane_id);
-    if (ok) fold<2>(tl, S, E);
-    if (ok) ok = wait_bar(st, 3, lane_id);
-    if (ok) fold<3>(tl + 64u, S, E);
-    if (ok) ok = wait_bar(st, 4, lane_id);
-    if (ok) fold<3>(tl + 128u, S, E);
-    if (ok) ok = wait_bar(st, 5, lane_id);
-    if (ok) fold<1>(tl + 192u, S, E);
+    const uint32_t tl = st.tmem + lane + (uint32_t)(2 * NA * h);
+    // round 4 (D0)
+    ok = wait_bar(st, 1, lane_id);
+    if (ok) {
+        fold<0>(tl, S, E);
+        fence_before();
+        __syncwarp();
+        if (lane_id == 0) mbar_arrive(st.bar + 24u);
+    }
+    // round 3 (D1)
+    if (ok) ok = wait_bar(st, 2, lane_id);
+    if (ok) {
+        fold<1>(tl + kD1, S, E);
+        fence_before();
+        __syncwarp();
+        if (lane_id == 0) mbar_arrive(st.bar + 32u);
+        // each issuer has already arrived for its own warp
+        if (tid == 0) {
+            if (wait_bar1(st, 3)) issue_round<1>(st.tmem, 0u, b0, st.bar + 8u);
+            else ok = false;
+        } else if (tid == 128) {
+            if (wait_bar1(st, 4)) issue_round<2>(st.tmem, kD1, b0, st.bar + 16u);
+            else ok = false;
+        }
+    }
+    st.ph ^= (1u << 3) | (1u << 4);
+    // round 2 (D1); once it has completed, round 0 goes into D2
+    if (ok) ok = wait_bar(st, 2, lane_id);
+    if (ok) {
+        if (tid == 128) issue_round<0>(st.tmem, kD2, b0, st.bar + 48u);
+        fold<2>(tl + kD1, S, E);
+    }
+    // round 1 (D0), round 0 (D2)
+    if (ok) ok = wait_bar(st, 1, lane_id);
+    if (ok) fold<3>(tl, S, E);
     if (ok) ok = wait_bar(st, 6, lane_id);
     if (ok) {
-        st.mma_out = false;
-        fold<1>(tl + 256u, S, E);
+        // every MMA of this gate has completed: sB takes the next gate's digit slices
+        if (tid == 128 && gnext) copy_slices(su32(sB), *s_nsrc, st.bar);
+        fold<3>(tl + kD2, S, E);
     }
-    st.pref = gnext != nullptr;
-    st.buf = buf ^ 1;
+    st.pref = ok && gnext != nullptr;
     if (!ok) {
         *s_fail = 1;
         atomicExch(err, 1);
         return;
     }
-    fence_before();   // the TMEM reads of this gate complete before the next gate's stores (after a barrier)
     const f2 osc2 = pk(osc, osc);
     float mx = 0.f;   // largest |high word|: its exponent field is the largest exponent field
 #pragma unroll

@@ -47,9 +47,6 @@ __device__ __forceinline__ cff f4c(float4 v) { return {v.x, v.z, v.y, v.w}; }
 __device__ __forceinline__ float4 c4f(const cff& c) { return make_float4(c.rh, c.ih, c.rl, c.il); }
 __device__ __forceinline__ cff f4m(float4 v) { return {v.x, v.y, v.z, v.w}; }
 
-// Dense gate on K tile bits in packed complex float-float (bs_ff.cuh: pacc): the real and
-// imaginary halves of each complex sum share one register pair, so one f32x2 instruction does the
-// work of two scalar ones, with the roundings of the scalar sequence in each half.
 template <int K, bool SW = false>
 __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* __restrict__ mats) {
     constexpr int D = 1 << K;
@@ -69,31 +66,23 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
 #pragma unroll
     for (int q = 0; q < K; q++) tb[q] = g.tbit[q];
     if (K == 1) {
-        // 2x2: packed coefficients held in registers across the thread's pairs
-        pcoef A[4], B[4];
-#pragma unroll
-        for (int e = 0; e < 4; e++) pcoefs(__ldg(m + e), A[e], B[e]);
+        // 2x2: matrix held in registers across the thread's pairs
+        const cff m00 = f4m(__ldg(m)), m01 = f4m(__ldg(m + 1)), m10 = f4m(__ldg(m + 2)), m11 = f4m(__ldg(m + 3));
         const int b0 = 1 << tb[0];
 #pragma unroll 2
         for (int gr = threadIdx.x; gr < ngroups; gr += blockDim.x) {
             const int jb = insert0(gr, pos[0]);
             if ((jb & (int)lcm) != (int)lcv) continue;
             const int ia = sx<SW>(jb), ib = sx<SW>(jb | b0);
-            f2 ah, al, bh, bl;
-            split4(sm[ia], ah, al);
-            split4(sm[ib], bh, bl);
-            const f2 ash = swap2(ah), asl = swap2(al), bsh = swap2(bh), bsl = swap2(bl);
-            pacc y;
-            f2 yh, yl;
-            pcmac_first(y, A[0], B[0], ah, al, ash, asl);
-            pcmac(y, A[1], B[1], bh, bl, bsh, bsl);
-            pacc_done(y, yh, yl);
-            pcmac_first(y, A[2], B[2], ah, al, ash, asl);
-            pcmac(y, A[3], B[3], bh, bl, bsh, bsl);
-            f2 zh, zl;
-            pacc_done(y, zh, zl);
-            sm[ib] = join4(zh, zl);
-            sm[ia] = join4(yh, yl);
+            const cff a = f4c(sm[ia]), b = f4c(sm[ib]);
+            ffacc ar, ai;
+            cmac_first(ar, ai, m00, a);
+            cmac(ar, ai, m01, b);
+            const cff ya = cdone(ar, ai);
+            cmac_first(ar, ai, m10, a);
+            cmac(ar, ai, m11, b);
+            sm[ib] = c4f(cdone(ar, ai));
+            sm[ia] = c4f(ya);
         }
         return;
     }
@@ -102,7 +91,7 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
 #pragma unroll
         for (int q = 0; q < K; q++) jb = insert0(jb, pos[q]);
         if ((jb & (int)lcm) != (int)lcv) continue;
-        f2 xh[D], xl[D];
+        cff x[D];
         int idx[D];
 #pragma unroll
         for (int c = 0; c < D; c++) {
@@ -110,22 +99,15 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
 #pragma unroll
             for (int q = 0; q < K; q++) if ((c >> q) & 1) j |= 1 << tb[q];
             idx[c] = sx<SW>(j);
-            split4(sm[idx[c]], xh[c], xl[c]);
+            x[c] = f4c(sm[idx[c]]);
         }
 #pragma unroll
         for (int r = 0; r < D; r++) {
-            pacc y;
-            pcoef A, B;
-            pcoefs(__ldg(m + r * D), A, B);
-            pcmac_first(y, A, B, xh[0], xl[0], swap2(xh[0]), swap2(xl[0]));
+            ffacc ar, ai;
+            cmac_first(ar, ai, f4m(__ldg(m + r * D)), x[0]);
 #pragma unroll
-            for (int c = 1; c < D; c++) {
-                pcoefs(__ldg(m + r * D + c), A, B);
-                pcmac(y, A, B, xh[c], xl[c], swap2(xh[c]), swap2(xl[c]));
-            }
-            f2 yh, yl;
-            pacc_done(y, yh, yl);
-            sm[idx[r]] = join4(yh, yl);
+            for (int c = 1; c < D; c++) cmac(ar, ai, f4m(__ldg(m + r * D + c)), x[c]);
+            sm[idx[r]] = c4f(cdone(ar, ai));
         }
     }
 }
@@ -214,12 +196,7 @@ __device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const flo
             if (d.x == 0.f && d.z == 1.f) { sm[js] = c4f(cmul_ipow(f4c(sm[js]), 1)); continue; }
             if (d.x == 0.f && d.z == -1.f) { sm[js] = c4f(cmul_ipow(f4c(sm[js]), 3)); continue; }
         }
-        pcoef A, B;
-        pcoefs(d, A, B);
-        f2 xh, xl, yh, yl;
-        split4(sm[js], xh, xl);
-        pcmul(A, B, xh, xl, yh, yl);
-        sm[js] = join4(yh, yl);
+        sm[js] = c4f(cmul(f4m(d), f4c(sm[js])));
     }
 }
 
@@ -397,10 +374,10 @@ __global__ void __launch_bounds__(NT) k_tile_sweep(double2* __restrict__ psi, Sw
 // fused gate), so one CTA's MMAs overlap the other's CUDA-core work.  The tile is stored with the
 // bank swizzle tc::sw.
 #ifndef BS_TC_THREADS
-#define BS_TC_THREADS 512
+#define BS_TC_THREADS 256
 #endif
-constexpr int kTcThreads = BS_TC_THREADS;   // one CTA of 16 warps per SM (128 registers each)
-constexpr int kTcSmem = 2 * 49152 + 65536;   // two digit-slice buffers and the tile: one CTA per SM
+constexpr int kTcThreads = BS_TC_THREADS;   // 256 (128 registers) or 512 (64 registers, spills; measured slower)
+constexpr int kTcSmem = 49152 + 65536;
 
 // Global offset (>> 5) of the tile's high-bit pattern i (7 bits) from two small tables:
 // a[i & 7] | b[i >> 3].
@@ -410,13 +387,13 @@ struct HiOff {
     __device__ __forceinline__ uint32_t operator[](int i) const { return a[i & 7] | b[i >> 3]; }
 };
 
-__global__ void __launch_bounds__(kTcThreads, 1) k_tile_sweep_tc(double2* __restrict__ psi, SweepDesc d, int64_t tile0,
+__global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __restrict__ psi, SweepDesc d, int64_t tile0,
                                                                  int tc_last) {
     // 128-byte alignment: each 128-byte core matrix of the matrix operand sits in one shared-memory line
     extern __shared__ __align__(128) unsigned char dsm[];
-    uint16_t* sB = reinterpret_cast<uint16_t*>(dsm);                 // two 48 KiB digit-slice buffers
-    float4* smem = reinterpret_cast<float4*>(dsm + 2 * 49152);
-    __shared__ __align__(8) uint64_t bars[7];   // digit copies into buffers 0 / 1, MMAs of rounds 0..4 done
+    uint16_t* sB = reinterpret_cast<uint16_t*>(dsm);
+    float4* smem = reinterpret_cast<float4*>(dsm + 49152);
+    __shared__ __align__(8) uint64_t bars[7];   // digit copy, MMAs into D0 / D1, D0 / D1 read, D1 free, D2
     __shared__ uint32_t s_tmem;
     __shared__ int64_t s_base;
     __shared__ int s_fail;
@@ -425,6 +402,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tile_sweep_tc(double2* __rest
     __shared__ uint32_t s_wmax[kTcThreads / 32];   // per-warp largest high-word exponent field
     __shared__ int s_act[32], s_cnt;                 // kind 5: blocks passing the row/column test
     __shared__ int s_tcq[16], s_ntc;                 // the tile's first 16 fused gates, in order
+    __shared__ const uint16_t* s_nsrc;
     const HiOff off32{s_offa, s_offb};
     constexpr int T = 12, L = 5, H = 7, nt = 1 << T, lowmask = (1 << L) - 1;
     const int64_t tile = tile0 + (int64_t)blockIdx.x;
@@ -435,7 +413,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tile_sweep_tc(double2* __rest
             if (!((d.tile_mask >> bit) & 1ULL)) { base |= ((tile >> src) & 1LL) << bit; src++; }
         s_base = base;
         s_fail = 0;
-        for (int b = 0; b < 7; b++) tc::mbar_init(tc::su32(&bars[b]));
+        tc::mbar_init(tc::su32(&bars[0]));
+        tc::mbar_init(tc::su32(&bars[1]));
+        tc::mbar_init(tc::su32(&bars[2]));
+        tc::mbar_init_n(tc::su32(&bars[3]), kTcThreads / 32);
+        tc::mbar_init_n(tc::su32(&bars[4]), kTcThreads / 32);
+        tc::mbar_init(tc::su32(&bars[5]));
+        tc::mbar_init(tc::su32(&bars[6]));
     }
     if (threadIdx.x < 24) {
         const int i = threadIdx.x < 8 ? threadIdx.x : (threadIdx.x - 8) << 3;
@@ -493,7 +477,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tile_sweep_tc(double2* __rest
         if ((threadIdx.x & 31) == 0) s_wmax[threadIdx.x >> 5] = eb;
     }
     __syncthreads();
-    tc::State st{0u, tc::su32(&bars[0]), 0u, s_ntc > 0 ? 1u : 0u, 0, s_ntc > 0, false};
+    tc::State st{0u, tc::su32(&bars[0]), 0u, s_ntc > 0};
     int q = 0;   // fused gates run so far
     bool have = false;
     bool emax_ok = true;   // s_wmax holds the tile's largest exponent (no magnitude-changing gate since)
@@ -513,7 +497,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tile_sweep_tc(double2* __rest
                 have = true;
             }
             const TileGate* gn = q + 1 < s_ntc ? d.gates + s_tcq[q + 1] : nullptr;
-            tc::apply<kTcThreads>(smem, g, gn, d.tc_pool, sB, st, base, s_wmax, emax_ok, s_tsw, &s_fail, d.err);
+            tc::apply<kTcThreads>(smem, g, gn, d.tc_pool, sB, st, base, s_wmax, emax_ok, s_tsw, &s_nsrc, &s_fail,
+                                  d.err);
             q++;
             emax_ok = true;
             if (gi == tc_last) {
@@ -548,9 +533,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tile_sweep_tc(double2* __rest
     if (have) {
         // a wait gave up: give the copies and MMAs in flight a bounded time to land before releasing TMEM
         if (threadIdx.x == 0 && s_fail) {
-            for (int b = 0; b < 2; b++)
-                if ((st.inflight >> b) & 1u) tc::mbar_wait(st.bar + 8u * (uint32_t)b, (st.ph >> b) & 1u);
-            if (st.mma_out) tc::mbar_wait(st.bar + 48u, (st.ph >> 6) & 1u);
+            tc::mbar_wait(st.bar, st.ph & 1u);
+            tc::mbar_wait(st.bar + 8u, (st.ph >> 1) & 1u);
+            tc::mbar_wait(st.bar + 16u, (st.ph >> 2) & 1u);
+            tc::mbar_wait(st.bar + 48u, (st.ph >> 6) & 1u);
         }
         __syncthreads();
         if (warp == 0) tc::tmem_dealloc(st.tmem);
