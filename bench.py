@@ -757,6 +757,78 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def _only_adjoint(bs):
+    from importlib import import_module
+    adj = import_module("braketsimulator_gb300.adjoint")
+    ops, h = adjoint_workload(bs, n=24, layers=4)
+    sim = bs.StateVectorSimulator(24, 0)
+    for _ in range(3):
+        e, g = adj.adjoint_gradient(sim, ops, h)
+    return {"energy": e, "params": len(g)}
+
+
+def _only_expect(bs):
+    n = 26
+    sim = bs.StateVectorSimulator(n, 0).evolve(dense_circuit(bs, n=n, layers=2, layers2=0))
+    _, h = adjoint_workload(bs, n=n, layers=1, terms=48)
+    from importlib import import_module
+    adj = import_module("braketsimulator_gb300.adjoint")
+    xm = np.array([adj.pauli_masks(t)[0] for _, t in h], dtype=np.uint64)
+    zm = np.array([adj.pauli_masks(t)[1] for _, t in h], dtype=np.uint64)
+    co = np.array([c for c, _ in h])
+    out = np.empty(len(co))
+    for _ in range(3):
+        sim._h.call("bs_expectation_pauli", len(co), bs._abi.u64ptr(xm), bs._abi.u64ptr(zm), bs._abi.dptr(co),
+                    bs._abi.dptr(out))
+    return {"energy": float(out.sum())}
+
+
+def _only_sample(bs):
+    n = 26
+    sim = bs.StateVectorSimulator(n, SHOTS).evolve(dense_circuit(bs, n=n, layers=2, layers2=0))
+    for r in range(3):
+        s = sim.samples(r)
+    return {"distinct": int(np.unique(s).size)}
+
+
+def _only_batch_small(bs):
+    circuits, counts, obs = batch_circuits(bs, nc=256, seed=11)
+    keep = [c for c in range(len(counts)) if counts[c] <= 12] or [0]
+    for _ in range(3):
+        exp, smp, st = bs.batch_simulate([circuits[c] for c in keep], [counts[c] for c in keep], [obs[c] for c in keep],
+                                         shots=1000, seed=1, precision="c64")
+    return {"circuits": len(keep)}
+
+
+def _only_dense(bs):
+    n = 27
+    sim = bs.StateVectorSimulator(n, 0)
+    ops = dense_circuit(bs, n=n)
+    for _ in range(2):
+        sim.reinit(n, 0)
+        sim.evolve(ops)
+    return sim.last_stats()
+
+
+# side workloads for kernel profiles: (what runs, the kernel it exercises)
+PROFILE_WORKLOADS = {
+    "adjoint24": (_only_adjoint, "k_adjoint_sweep: 24-qubit Ry/Rz/ZZ ansatz, 4 layers, 48 terms (256 MiB state)"),
+    "expect26": (_only_expect, "k_pauli_sv: 48 Pauli terms on a 26-qubit state (1 GiB)"),
+    "sample26": (_only_sample, "k_block_sums / k_sample_rng: 1e5 shots of a 26-qubit state"),
+    "batch_small": (_only_batch_small, "k_batch_small: the <= 12-qubit circuits of a 256-circuit batch"),
+    "dense27": (_only_dense, "k_tile_sweep_tc: the dense circuit at 27 qubits (2 GiB state)"),
+}
+
+
+def run_only(name):
+    bs = load()
+    fn, what = PROFILE_WORKLOADS[name]
+    out = fn(bs)
+    import torch
+    torch.cuda.synchronize()
+    print(json.dumps({"only": name, "what": what, **{k: v for k, v in out.items() if isinstance(v, (int, float))}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -767,8 +839,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--qubits", type=int, default=N_QUBITS, help="smaller cases for profiling")
     ap.add_argument("--precision", default="c128", choices=["c128", "c64"])
+    ap.add_argument("--only", default=None, choices=sorted(PROFILE_WORKLOADS),
+                    help="run one side workload a few times and exit (the small cases the kernel profiles use)")
     args = ap.parse_args()
     globals()["N_QUBITS"] = args.qubits
+    if args.only:
+        return run_only(args.only)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))

@@ -64,6 +64,30 @@ struct OutStage {
     }
 };
 thread_local OutStage t_out;
+// Pinned host memory mapped into the device's address space, one per host thread: bs_run_small's
+// kernel writes the probabilities and the shots straight into it (no copy call), the host reads them
+// after the one synchronisation.
+struct MapStage {
+    char* h = nullptr;
+    char* d = nullptr;
+    bool tried = false;
+    ~MapStage() {
+        if (h) cudaFreeHost(h);
+    }
+};
+thread_local MapStage t_map;
+bool map_stage() {
+    if (t_map.h) return true;
+    if (t_map.tried) return false;
+    t_map.tried = true;
+    void* h = nullptr;
+    void* d = nullptr;
+    if (cudaHostAlloc(&h, kOutStage, cudaHostAllocMapped) != cudaSuccess) { cudaGetLastError(); return false; }
+    if (cudaHostGetDevicePointer(&d, h, 0) != cudaSuccess) { cudaGetLastError(); cudaFreeHost(h); return false; }
+    t_map.h = (char*)h;
+    t_map.d = (char*)d;
+    return true;
+}
 }  // namespace
 
 int bs_copy_out(bs_sim* s, void* host, const void* dev, size_t bytes, const char* what) {
@@ -516,7 +540,9 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
 }
 
 // simulate (src/BraketSimulator.jl:307-322: reinit!, evolve!, probabilities, samples) of one small
-// state-vector circuit as one upload, two launches and one synchronisation.
+// state-vector circuit as one upload, one launch and one synchronisation: the kernel evolves the
+// state in one CTA, writes it back, and writes the probabilities and the shots into mapped pinned
+// host memory.
 int bs_run_small(bs_sim* s, const bs_op* ops, int64_t n_ops, int64_t shots, uint64_t seed, double* probs_out,
                  int64_t* samples_out) {
     if (!s) return BS_ERR_INVALID_ARG;
@@ -533,12 +559,21 @@ int bs_run_small(bs_sim* s, const bs_op* ops, int64_t n_ops, int64_t shots, uint
     s->defer_sync = defer;
     s->collect = nullptr;
     if (rc) return rc;
-    rc = bs_ensure_scratch(s, dim * 8 + shots * 8 + 256);
-    if (rc) return rc;
-    double* dprobs = (double*)s->scratch;
-    int64_t* dsamp = (int64_t*)((char*)s->scratch + ((dim * 8 + 255) & ~(int64_t)255));
+    const size_t pb = ((size_t)dim * 8 + 255) & ~(size_t)255, sb = (size_t)shots * 8;
+    const bool mapped = pb + sb <= kOutStage && map_stage();
+    double* dprobs;
+    int64_t* dsamp;
+    if (mapped) {
+        dprobs = (double*)t_map.d;
+        dsamp = (int64_t*)(t_map.d + pb);
+    } else {
+        rc = bs_ensure_scratch(s, (int64_t)(pb + sb) + 256);
+        if (rc) return rc;
+        dprobs = (double*)s->scratch;
+        dsamp = (int64_t*)((char*)s->scratch + pb);
+    }
     cudaEventRecord(s->ev0, s->stream);
-    rc = bs_run_small_sweeps(s, sweeps, dprobs);
+    rc = bs_run_small_sweeps(s, sweeps, dprobs, shots, seed, dsamp);
     if (rc == BS_ERR_UNSUPPORTED) {
         // a gate without an in-tile kernel (dense on more than 4 qubits) or a complex64 state: the usual
         // path, with the same results
@@ -550,26 +585,16 @@ int bs_run_small(bs_sim* s, const bs_op* ops, int64_t n_ops, int64_t shots, uint
     }
     if (rc) return rc;
     s->alias_valid = false;
-    if (shots > 0) {
-        rc = bs_launch_sample_small(s, seed, shots, dsamp);
-        if (rc) return rc;
-    }
     cudaEventRecord(s->ev1, s->stream);
-    // results: one copy of [probabilities | samples] through the pinned per-thread buffer when it fits
-    const size_t pb = probs_out ? (size_t)dim * 8 : 0, sb = (size_t)shots * 8;
-    if (pb + sb <= kOutStage && (t_out.p || cudaMallocHost(&t_out.p, kOutStage) == cudaSuccess)) {
-        if (pb) cudaMemcpyAsync(t_out.p, dprobs, pb, cudaMemcpyDeviceToHost, s->stream);
-        if (sb) cudaMemcpyAsync((char*)t_out.p + pb, dsamp, sb, cudaMemcpyDeviceToHost, s->stream);
-        rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "small run");
-        if (rc) return rc;
-        if (pb) std::memcpy(probs_out, t_out.p, pb);
-        if (sb) std::memcpy(samples_out, (char*)t_out.p + pb, sb);
-    } else {
-        cudaGetLastError();
-        if (pb) cudaMemcpyAsync(probs_out, dprobs, pb, cudaMemcpyDeviceToHost, s->stream);
+    if (!mapped) {
+        if (probs_out) cudaMemcpyAsync(probs_out, dprobs, (size_t)dim * 8, cudaMemcpyDeviceToHost, s->stream);
         if (sb) cudaMemcpyAsync(samples_out, dsamp, sb, cudaMemcpyDeviceToHost, s->stream);
-        rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "small run");
-        if (rc) return rc;
+    }
+    rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "small run");
+    if (rc) return rc;
+    if (mapped) {
+        if (probs_out) std::memcpy(probs_out, t_map.h, (size_t)dim * 8);
+        if (sb) std::memcpy(samples_out, t_map.h + pb, sb);
     }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <thread>
@@ -324,6 +325,18 @@ void small_image(char* img, const SmallLayout& L, const std::vector<BCirc>& bc, 
 
 uint64_t circuit_seed(uint64_t seed, int c) { return seed ^ ((uint64_t)c * 0x9E3779B97F4A7C15ULL); }
 
+// Handles (one stream each) that run the larger circuits side by side: a circuit of 12 to 20 qubits
+// fills only a few CTAs per sweep, so many of them must run at once to fill the GPU
+// (BS_BATCH_STREAMS, default 16, at most 64).
+int batch_pool_size(size_t n_large) {
+    static const int cap = [] {
+        const char* v = getenv("BS_BATCH_STREAMS");
+        const int x = v ? atoi(v) : 16;
+        return std::max(1, std::min(64, x));
+    }();
+    return (int)std::min<size_t>(n_large, (size_t)cap);
+}
+
 void add_stats(bs_stats& a, const bs_stats& b) {
     a.sweeps += b.sweeps;
     a.kernel_launches += b.kernel_launches;
@@ -392,7 +405,7 @@ extern "C" int bs_run_batch(int n_circuits, const int* n_qubits, const bs_op* co
     std::atomic<int> next{0};
     std::atomic<int> err{0};
     std::sort(large.begin(), large.end(), [&](int a, int b) { return n_qubits[a] > n_qubits[b]; });
-    const int workers = (int)std::min<size_t>(large.size(), 4);
+    const int workers = batch_pool_size(large.size());
     std::vector<bs_stats> wst((size_t)std::max(workers, 1));
     int dev = 0;
     cudaGetDevice(&dev);
@@ -698,7 +711,7 @@ int bs_batch_create(int n_circuits, const int* n_qubits, const bs_op* const* ops
     for (int c = 0; c < n_circuits; c++) (small_ok(precision, n_qubits[c], ops[c], n_ops[c]) ? b->small : b->large).push_back(c);
     // largest first onto the handle with the least work so far (work ~ 2^n)
     std::sort(b->large.begin(), b->large.end(), [&](int x, int y) { return n_qubits[x] > n_qubits[y] || (n_qubits[x] == n_qubits[y] && x < y); });
-    const int workers = (int)std::min<size_t>(b->large.size(), 4);
+    const int workers = batch_pool_size(b->large.size());
     std::vector<double> load((size_t)workers, 0.0);
     std::vector<int> wmax((size_t)workers, 1);
     b->owner.assign((size_t)n_circuits, -1);

@@ -183,9 +183,9 @@ int64_t bs_alias_parallel_scratch(int64_t n);
 int bs_alias_parallel(bs_sim* s, const double* dprobs, int64_t n, double wsum, double* ap, int64_t* alias, void* work);
 
 // ---- small state vectors in one CTA (bs_tile.cu, bs_sample.cu)
-// |0...0>, the planned sweeps' gates, the state written back and its probabilities into dprobs (device);
-// BS_ERR_UNSUPPORTED (nothing launched) when a gate has no in-tile kernel or the state is not a
-// complex128 state vector of at most 12 qubits.
-int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dprobs);
-// k_sample_small's draws (bs_sample's generator) of a state of at most 4096 amplitudes into dout (device)
-int bs_launch_sample_small(bs_sim* s, uint64_t seed, int64_t shots, int64_t* dout);
+// |0...0>, the planned sweeps' gates, the state written back, its probabilities into dprobs and `shots`
+// draws of bs_sample's generator with `seed` into dsamples, in one launch (dprobs and dsamples: device
+// addresses, mapped host memory included); BS_ERR_UNSUPPORTED (nothing launched) when a gate has no
+// in-tile kernel or the state is not a complex128 state vector of at most 12 qubits.
+int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dprobs, int64_t shots, uint64_t seed,
+                        int64_t* dsamples);

@@ -16,6 +16,7 @@
 #include "bs_internal.h"
 #include "bs_ff.cuh"
 #include "bs_tc.cuh"
+#include "bs_cdf.cuh"
 
 namespace {
 
@@ -1692,8 +1693,11 @@ struct NoOff {
 template <int KMAX>
 __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, int n, const TileGate* __restrict__ gates,
                                                    int ng, const float4* __restrict__ mats,
-                                                   const int32_t* __restrict__ perms, double* __restrict__ probs) {
+                                                   const int32_t* __restrict__ perms, double* __restrict__ probs,
+                                                   int64_t shots, uint64_t seed, int64_t* __restrict__ samples) {
     extern __shared__ float4 smem[];
+    __shared__ float s_ch[kCpb], s_cl[kCpb];
+    __shared__ double s_cinc[kCpb], s_total;
     const int nt = 1 << n;
     for (int j = threadIdx.x; j < nt; j += blockDim.x) smem[j] = make_float4(j == 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
     __syncthreads();
@@ -1725,11 +1729,52 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
         const ff r = acc_done(a);
         probs[j] = ff2d(r.h, r.l);
     }
+    __syncthreads();   // the state just written is read back below (global writes of this CTA, visible after the barrier)
+    if (shots <= 0) return;
+    // The shots, as bs_sample draws them for a state of one CDF block (k_sample_small): the same
+    // chunk sums and chunk prefix sums, the same in-chunk running sums (a warp's shuffle scan, kept
+    // here per element), the same uniforms and comparisons, so the same indices; one thread per shot.
+    block_chunk_sums(psi, 0, nt, 0, s_ch, s_cl, &s_total, s_cinc);
+    double* scan = reinterpret_cast<double*>(smem);   // the tile is no longer needed
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int c = warp; c * kChunk < nt; c += nw) {
+        const int i = c * kChunk + lane;
+        double p = (i < nt) ? prob_at(psi, 0, nt, i) : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double v = __shfl_up_sync(0xffffffffu, p, o);
+            if (lane >= o) p += v;
+        }
+        scan[i] = p;
+    }
+    __syncthreads();
+    const double total = 0.0 + s_total;
+    for (int64_t sh = threadIdx.x; sh < shots; sh += blockDim.x) {
+        const uint64_t r = splitmix64(seed ^ splitmix64((uint64_t)sh));
+        const double t = (double)(r >> 11) * 0x1.0p-53 * total;
+        int clo = 0, chi = kCpb - 1;
+        while (clo < chi) {
+            const int mid = (clo + chi) >> 1;
+            if (0.0 + s_cinc[mid] >= t) chi = mid; else clo = mid + 1;
+        }
+        double cw = 0.0 + (clo == 0 ? 0.0 : s_cinc[clo - 1]);
+        int64_t out = nt - 1;
+        bool found = false;
+        for (int c = clo * kChunk; c < nt && !found; c += kChunk) {
+            for (int l = 0; l < kChunk; l++) {
+                const int i = c + l;
+                if (i < nt && cw + scan[i] >= t) { out = i; found = true; break; }
+            }
+            cw += scan[c + kChunk - 1];
+        }
+        samples[sh] = out;
+    }
 }
 
 }  // namespace
 
-int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dprobs) {
+int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dprobs, int64_t shots, uint64_t seed,
+                        int64_t* dsamples) {
     const int n = s->n;
     if (s->kind != BS_KIND_SV || s->precision != BS_PREC_C128 || n > 12) return BS_ERR_UNSUPPORTED;
     std::vector<TileGate> tg;
@@ -1781,7 +1826,8 @@ int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dpr
                        "plan upload");
     bs_stage_done(s);
     if (rc) return rc;
-    const size_t smem = ((size_t)1 << n) * sizeof(float4);
+    // the tile, and afterwards the per-element running sums of the sampler (whole 32-element chunks)
+    const size_t smem = std::max(((size_t)1 << n) * sizeof(float4), (size_t)(((1 << n) + 31) / 32 * 32) * sizeof(double));
     const TileGate* d_tg = (const TileGate*)dev;
     const float4* d_m = (const float4*)(dev + b_tg);
     const int32_t* d_p = (const int32_t*)(dev + b_tg + b_m);
@@ -1791,11 +1837,13 @@ int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dpr
         cudaFuncSetAttribute(k_small_run<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
         attr_set[s->device & 63] = true;
     }
-    const int threads = std::min(512, std::max(32, (1 << n) / 2));
+    const int threads = std::min(512, std::max(128, (1 << n) / 2));
     if (kmax <= 2)
-        k_small_run<2><<<1, threads, smem, s->stream>>>((double2*)s->state, n, d_tg, (int)tg.size(), d_m, d_p, dprobs);
+        k_small_run<2><<<1, threads, smem, s->stream>>>((double2*)s->state, n, d_tg, (int)tg.size(), d_m, d_p, dprobs,
+                                                        shots, seed, dsamples);
     else
-        k_small_run<4><<<1, threads, smem, s->stream>>>((double2*)s->state, n, d_tg, (int)tg.size(), d_m, d_p, dprobs);
+        k_small_run<4><<<1, threads, smem, s->stream>>>((double2*)s->state, n, d_tg, (int)tg.size(), d_m, d_p, dprobs,
+                                                        shots, seed, dsamples);
     s->stats.kernel_launches++;
     s->stats.sweeps++;
     s->stats.gates += (int64_t)tg.size();

@@ -54,7 +54,7 @@ def test_run_repeats_and_resets():
     p2, s2 = sim.run(ops, 200, seed=11)
     assert np.array_equal(p1, p2) and np.array_equal(s1, s2)
     ref = oracle.OracleSV(6).evolve(ops).psi
-    assert np.max(np.abs(p1 - np.abs(ref) ** 2)) < 1e-15
+    assert np.max(np.abs(p1 - np.abs(ref) ** 2)) < 1e-14
 
 
 def test_run_falls_back_for_wide_gates_and_complex64():
