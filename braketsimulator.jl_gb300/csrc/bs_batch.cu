@@ -325,13 +325,13 @@ void small_image(char* img, const SmallLayout& L, const std::vector<BCirc>& bc, 
 
 uint64_t circuit_seed(uint64_t seed, int c) { return seed ^ ((uint64_t)c * 0x9E3779B97F4A7C15ULL); }
 
-// Handles (one stream each) that run the larger circuits side by side: a circuit of 12 to 20 qubits
-// fills only a few CTAs per sweep, so many of them must run at once to fill the GPU
-// (BS_BATCH_STREAMS, default 16, at most 64).
+// Handles (one stream each) that run the larger circuits side by side (BS_BATCH_STREAMS, default 4, at
+// most 64).  On the 512-circuit benchmark batch 4, 16 and 32 streams replay in the same 1.30-1.31 s:
+// the largest circuits' sweeps, which fill the GPU on their own, set the time.
 int batch_pool_size(size_t n_large) {
     static const int cap = [] {
         const char* v = getenv("BS_BATCH_STREAMS");
-        const int x = v ? atoi(v) : 16;
+        const int x = v ? atoi(v) : 4;
         return std::max(1, std::min(64, x));
     }();
     return (int)std::min<size_t>(n_large, (size_t)cap);

@@ -227,7 +227,7 @@ int bs_run_batch(int n_circuits, const int* n_qubits, const bs_op* const* ops, c
 
 /* ---- captured batches.  The same work as bs_run_batch (same results, same per-circuit shot
  * seeds), captured once into a CUDA graph and replayed: bs_batch_create runs the batch eagerly once
- * (sizing a pool of handles, 16 by default (BS_BATCH_STREAMS), circuits assigned largest-first), then captures every
+ * (sizing a pool of handles, 4 by default (BS_BATCH_STREAMS), circuits assigned largest-first), then captures every
  * upload, kernel and result copy of the batch into one graph; bs_batch_launch replays it and
  * copies the results out (host work per replay: one graph launch and two memcpy).
  * bs_batch_set_ops replaces every circuit's ops (same qubit counts; a circuit may not move
