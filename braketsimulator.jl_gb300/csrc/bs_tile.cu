@@ -1736,6 +1736,8 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
     // here per element), the same uniforms and comparisons, so the same indices; one thread per shot.
     block_chunk_sums(psi, 0, nt, 0, s_ch, s_cl, &s_total, s_cinc);
     double* scan = reinterpret_cast<double*>(smem);   // the tile is no longer needed
+    const int nc32 = (nt + kChunk - 1) / kChunk * kChunk;
+    double* first = scan + nc32;                        // what a search compares in its first chunk
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int c = warp; c * kChunk < nt; c += nw) {
         const int i = c * kChunk + lane;
@@ -1746,26 +1748,37 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
             if (lane >= o) p += v;
         }
         scan[i] = p;
+        first[i] = (0.0 + (c == 0 ? 0.0 : s_cinc[c - 1])) + p;
     }
     __syncthreads();
+    // Every value compared below is a sum of probabilities, so non-negative: its order is the order of
+    // its bit pattern as an integer, which keeps the comparisons off the FP64 pipe (2 per clock per SM).
     const double total = 0.0 + s_total;
     for (int64_t sh = threadIdx.x; sh < shots; sh += blockDim.x) {
         const uint64_t r = splitmix64(seed ^ splitmix64((uint64_t)sh));
         const double t = (double)(r >> 11) * 0x1.0p-53 * total;
+        const long long tb = __double_as_longlong(t);
         int clo = 0, chi = kCpb - 1;
         while (clo < chi) {
             const int mid = (clo + chi) >> 1;
-            if (0.0 + s_cinc[mid] >= t) chi = mid; else clo = mid + 1;
+            if (__double_as_longlong(0.0 + s_cinc[mid]) >= tb) chi = mid; else clo = mid + 1;
         }
-        double cw = 0.0 + (clo == 0 ? 0.0 : s_cinc[clo - 1]);
         int64_t out = nt - 1;
         bool found = false;
-        for (int c = clo * kChunk; c < nt && !found; c += kChunk) {
-            for (int l = 0; l < kChunk; l++) {
-                const int i = c + l;
-                if (i < nt && cw + scan[i] >= t) { out = i; found = true; break; }
+        const int c0 = clo * kChunk;
+        for (int l = 0; l < kChunk && c0 + l < nt; l++)
+            if (__double_as_longlong(first[c0 + l]) >= tb) { out = c0 + l; found = true; break; }
+        if (!found && c0 < nt) {
+            // the chunk's own running sum fell short of its prefix sum by rounding: go on as the
+            // one-block sampler does, with the running sum carried from chunk to chunk
+            double cw = (0.0 + (clo == 0 ? 0.0 : s_cinc[clo - 1])) + scan[c0 + kChunk - 1];
+            for (int c = c0 + kChunk; c < nt && !found; c += kChunk) {
+                for (int l = 0; l < kChunk; l++) {
+                    const int i = c + l;
+                    if (i < nt && cw + scan[i] >= t) { out = i; found = true; break; }
+                }
+                cw += scan[c + kChunk - 1];
             }
-            cw += scan[c + kChunk - 1];
         }
         samples[sh] = out;
     }
@@ -1826,8 +1839,8 @@ int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dpr
                        "plan upload");
     bs_stage_done(s);
     if (rc) return rc;
-    // the tile, and afterwards the per-element running sums of the sampler (whole 32-element chunks)
-    const size_t smem = std::max(((size_t)1 << n) * sizeof(float4), (size_t)(((1 << n) + 31) / 32 * 32) * sizeof(double));
+    // the tile, and afterwards two arrays of the sampler (whole 32-element chunks)
+    const size_t smem = std::max(((size_t)1 << n) * sizeof(float4), (size_t)2 * (((1 << n) + 31) / 32 * 32) * sizeof(double));
     const TileGate* d_tg = (const TileGate*)dev;
     const float4* d_m = (const float4*)(dev + b_tg);
     const int32_t* d_p = (const int32_t*)(dev + b_tg + b_m);
