@@ -1,5 +1,7 @@
 // C ABI entry points: handle lifecycle, state transfer, gate / channel / evolve.
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cstring>
 #include <new>
 #include "bs_internal.h"
@@ -71,6 +73,7 @@ struct MapStage {
     char* h = nullptr;
     char* d = nullptr;
     bool tried = false;
+    int64_t ticket = 0;   // bs_run_small calls of this thread: the kernel writes the call's ticket when done
     ~MapStage() {
         if (h) cudaFreeHost(h);
     }
@@ -559,13 +562,18 @@ int bs_run_small(bs_sim* s, const bs_op* ops, int64_t n_ops, int64_t shots, uint
     s->defer_sync = defer;
     s->collect = nullptr;
     if (rc) return rc;
+    // mapped layout: the completion word (256 bytes), the probabilities, the shots
     const size_t pb = ((size_t)dim * 8 + 255) & ~(size_t)255, sb = (size_t)shots * 8;
-    const bool mapped = pb + sb <= kOutStage && map_stage();
+    const bool mapped = 256 + pb + sb <= kOutStage && map_stage();
     double* dprobs;
     int64_t* dsamp;
+    int64_t* ddone = nullptr;
+    int64_t ticket = 0;
     if (mapped) {
-        dprobs = (double*)t_map.d;
-        dsamp = (int64_t*)(t_map.d + pb);
+        ddone = (int64_t*)t_map.d;
+        ticket = ++t_map.ticket;
+        dprobs = (double*)(t_map.d + 256);
+        dsamp = (int64_t*)(t_map.d + 256 + pb);
     } else {
         rc = bs_ensure_scratch(s, (int64_t)(pb + sb) + 256);
         if (rc) return rc;
@@ -573,7 +581,7 @@ int bs_run_small(bs_sim* s, const bs_op* ops, int64_t n_ops, int64_t shots, uint
         dsamp = (int64_t*)((char*)s->scratch + pb);
     }
     cudaEventRecord(s->ev0, s->stream);
-    rc = bs_run_small_sweeps(s, sweeps, dprobs, shots, seed, dsamp);
+    rc = bs_run_small_sweeps(s, sweeps, dprobs, shots, seed, dsamp, ddone, ticket);
     if (rc == BS_ERR_UNSUPPORTED) {
         // a gate without an in-tile kernel (dense on more than 4 qubits) or a complex64 state: the usual
         // path, with the same results
@@ -589,17 +597,33 @@ int bs_run_small(bs_sim* s, const bs_op* ops, int64_t n_ops, int64_t shots, uint
     if (!mapped) {
         if (probs_out) cudaMemcpyAsync(probs_out, dprobs, (size_t)dim * 8, cudaMemcpyDeviceToHost, s->stream);
         if (sb) cudaMemcpyAsync(samples_out, dsamp, sb, cudaMemcpyDeviceToHost, s->stream);
+        rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "small run");
+        if (rc) return rc;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+        s->stats.gpu_ms = ms;
+        s->stats_pending = false;
+        return BS_OK;
     }
-    rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "small run");
-    if (rc) return rc;
-    if (mapped) {
-        if (probs_out) std::memcpy(probs_out, t_map.h, (size_t)dim * 8);
-        if (sb) std::memcpy(samples_out, t_map.h + pb, sb);
+    // Wait for the kernel's completion word rather than synchronising the stream (a round trip through
+    // the driver that costs more than the kernel): the kernel writes the ticket after every result is
+    // visible to the host.  A ticket that has not arrived after 2 s (a failed kernel) falls back to the
+    // stream synchronisation, which reports the error.
+    volatile int64_t* word = reinterpret_cast<volatile int64_t*>(t_map.h);
+    const auto t0 = std::chrono::steady_clock::now();
+    bool seen = false;
+    for (uint32_t it = 0;; it++) {
+        if (*word == ticket) { seen = true; break; }
+        if ((it & 1023u) == 1023u && std::chrono::steady_clock::now() - t0 > std::chrono::seconds(2)) break;
     }
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
-    s->stats.gpu_ms = ms;
-    s->stats_pending = false;
+    std::atomic_thread_fence(std::memory_order_acquire);
+    if (!seen) {
+        rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "small run");
+        if (rc) return rc;
+    }
+    if (probs_out) std::memcpy(probs_out, t_map.h + 256, (size_t)dim * 8);
+    if (sb) std::memcpy(samples_out, t_map.h + 256 + pb, sb);
+    s->stats_pending = true;   // the end event may still be on its way: bs_last_stats waits for it
     return BS_OK;
 }
 

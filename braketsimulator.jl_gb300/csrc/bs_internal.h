@@ -185,7 +185,9 @@ int bs_alias_parallel(bs_sim* s, const double* dprobs, int64_t n, double wsum, d
 // ---- small state vectors in one CTA (bs_tile.cu, bs_sample.cu)
 // |0...0>, the planned sweeps' gates, the state written back, its probabilities into dprobs and `shots`
 // draws of bs_sample's generator with `seed` into dsamples, in one launch (dprobs and dsamples: device
-// addresses, mapped host memory included); BS_ERR_UNSUPPORTED (nothing launched) when a gate has no
-// in-tile kernel or the state is not a complex128 state vector of at most 12 qubits.
+// addresses, mapped host memory included); at its end the kernel writes `ticket` into *done (a
+// host-mapped word, may be null) once every result is visible to the host.  BS_ERR_UNSUPPORTED
+// (nothing launched) when a gate has no in-tile kernel or the state is not a complex128 state vector
+// of at most 12 qubits.
 int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dprobs, int64_t shots, uint64_t seed,
-                        int64_t* dsamples);
+                        int64_t* dsamples, int64_t* done, int64_t ticket);

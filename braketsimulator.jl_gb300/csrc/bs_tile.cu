@@ -1690,14 +1690,25 @@ struct NoOff {
     __device__ __forceinline__ int64_t operator[](int) const { return 0; }
 };
 
+// The end of a small run, for a host that polls instead of synchronising: every thread's writes are
+// made visible to the system, then one thread writes the call's ticket into the host-mapped word.
+__device__ __forceinline__ void small_run_done(volatile int64_t* done, int64_t ticket) {
+    if (!done) return;
+    __threadfence_system();
+    __syncthreads();
+    if (threadIdx.x == 0) *done = ticket;
+}
+
 template <int KMAX>
 __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, int n, const TileGate* __restrict__ gates,
                                                    int ng, const float4* __restrict__ mats,
                                                    const int32_t* __restrict__ perms, double* __restrict__ probs,
-                                                   int64_t shots, uint64_t seed, int64_t* __restrict__ samples) {
+                                                   int64_t shots, uint64_t seed, int64_t* __restrict__ samples,
+                                                   volatile int64_t* done, int64_t ticket) {
     extern __shared__ float4 smem[];
     __shared__ float s_ch[kCpb], s_cl[kCpb];
     __shared__ double s_cinc[kCpb], s_total;
+    __shared__ long long s_ckey[kCpb];
     const int nt = 1 << n;
     for (int j = threadIdx.x; j < nt; j += blockDim.x) smem[j] = make_float4(j == 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
     __syncthreads();
@@ -1730,7 +1741,10 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
         probs[j] = ff2d(r.h, r.l);
     }
     __syncthreads();   // the state just written is read back below (global writes of this CTA, visible after the barrier)
-    if (shots <= 0) return;
+    if (shots <= 0) {
+        small_run_done(done, ticket);
+        return;
+    }
     // The shots, as bs_sample draws them for a state of one CDF block (k_sample_small): the same
     // chunk sums and chunk prefix sums, the same in-chunk running sums (a warp's shuffle scan, kept
     // here per element), the same uniforms and comparisons, so the same indices; one thread per shot.
@@ -1750,6 +1764,7 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
         scan[i] = p;
         first[i] = (0.0 + (c == 0 ? 0.0 : s_cinc[c - 1])) + p;
     }
+    for (int c = threadIdx.x; c < kCpb; c += blockDim.x) s_ckey[c] = __double_as_longlong(0.0 + s_cinc[c]);
     __syncthreads();
     // Every value compared below is a sum of probabilities, so non-negative: its order is the order of
     // its bit pattern as an integer, which keeps the comparisons off the FP64 pipe (2 per clock per SM).
@@ -1761,7 +1776,7 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
         int clo = 0, chi = kCpb - 1;
         while (clo < chi) {
             const int mid = (clo + chi) >> 1;
-            if (__double_as_longlong(0.0 + s_cinc[mid]) >= tb) chi = mid; else clo = mid + 1;
+            if (s_ckey[mid] >= tb) chi = mid; else clo = mid + 1;
         }
         int64_t out = nt - 1;
         bool found = false;
@@ -1782,12 +1797,13 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
         }
         samples[sh] = out;
     }
+    small_run_done(done, ticket);
 }
 
 }  // namespace
 
 int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dprobs, int64_t shots, uint64_t seed,
-                        int64_t* dsamples) {
+                        int64_t* dsamples, int64_t* done, int64_t ticket) {
     const int n = s->n;
     if (s->kind != BS_KIND_SV || s->precision != BS_PREC_C128 || n > 12) return BS_ERR_UNSUPPORTED;
     std::vector<TileGate> tg;
@@ -1853,10 +1869,10 @@ int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dpr
     const int threads = std::min(512, std::max(128, (1 << n) / 2));
     if (kmax <= 2)
         k_small_run<2><<<1, threads, smem, s->stream>>>((double2*)s->state, n, d_tg, (int)tg.size(), d_m, d_p, dprobs,
-                                                        shots, seed, dsamples);
+                                                        shots, seed, dsamples, done, ticket);
     else
         k_small_run<4><<<1, threads, smem, s->stream>>>((double2*)s->state, n, d_tg, (int)tg.size(), d_m, d_p, dprobs,
-                                                        shots, seed, dsamples);
+                                                        shots, seed, dsamples, done, ticket);
     s->stats.kernel_launches++;
     s->stats.sweeps++;
     s->stats.gates += (int64_t)tg.size();
