@@ -84,6 +84,55 @@ __device__ __forceinline__ void block_chunk_sums(const double2* __restrict__ st,
     __syncthreads();
 }
 
+// The same sums from probabilities already formed (prob_at's values, e.g. kept in shared memory).
+__device__ __forceinline__ void block_chunk_sums_p(const double* __restrict__ probs, int64_t dim, int64_t b,
+                                                 float* ch, float* cl, double* bsum, double* cinc) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nw = (int)(blockDim.x >> 5);
+    for (int c = warp; c < kCpb; c += nw) {
+        if (b * kBlk + (int64_t)c * kChunk >= dim) {   // past the end: an empty chunk sums to zero
+            if (lane == 0) { ch[c] = 0.f; cl[c] = 0.f; }
+            continue;
+        }
+        const int64_t i = b * kBlk + (int64_t)c * kChunk + lane;
+        ffsum a{0.f, 0.f};
+        if (i < dim) {
+            const ff f = d2ff(probs[i]);
+            a.h = f.h;
+            a.l = f.l;
+        }
+        ff_warp_sum(a);
+        if (lane == 0) { ch[c] = a.h; cl[c] = a.l; }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        // lane holds chunks 4 lane .. 4 lane + 3: local inclusive sums, then a warp scan of the totals
+        ffsum loc[4];
+        ffsum run{0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            fsum_add(run, ch[4 * lane + k], cl[4 * lane + k]);
+            loc[k] = run;
+        }
+        ffsum pre = run;   // inclusive scan of the lane totals
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float h = __shfl_up_sync(0xffffffffu, pre.h, o), l = __shfl_up_sync(0xffffffffu, pre.l, o);
+            if (lane >= o) fsum_add(pre, h, l);
+        }
+        ffsum off{__shfl_up_sync(0xffffffffu, pre.h, 1), __shfl_up_sync(0xffffffffu, pre.l, 1)};
+        if (lane == 0) off = ffsum{0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            ffsum v = off;
+            fsum_add(v, loc[k].h, loc[k].l);
+            cinc[4 * lane + k] = ff2d(v.h, v.l);
+        }
+        if (lane == 31) *bsum = ff2d(pre.h, pre.l);
+    }
+    __syncthreads();
+}
+
 __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
     x += 0x9e3779b97f4a7c15ULL;
     x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ULL;

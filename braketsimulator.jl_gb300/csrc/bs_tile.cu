@@ -1709,11 +1709,14 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
     __shared__ float s_ch[kCpb], s_cl[kCpb];
     __shared__ double s_cinc[kCpb], s_total;
     __shared__ long long s_ckey[kCpb];
-    const int nt = 1 << n;
+    __shared__ TileGate s_gates[kGateChunk];
+    const int nt = 1 << n, nc32 = (nt + kChunk - 1) / kChunk * kChunk;
+    // the probabilities, after the tile (or after the sampler's two arrays, which replace the tile)
+    double* sprob = reinterpret_cast<double*>(reinterpret_cast<char*>(smem) + max(nt * 16, 2 * nc32 * 8));
     for (int j = threadIdx.x; j < nt; j += blockDim.x) smem[j] = make_float4(j == 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
-    __syncthreads();
     for (int gi = 0; gi < ng; gi++) {
-        const TileGate& g = gates[gi];
+        if (gi % kGateChunk == 0) stage_gates(s_gates, gates + gi, min(kGateChunk, ng - gi));   // one latency per 32 gates
+        const TileGate& g = s_gates[gi % kGateChunk];
         const int kind = g.kind, k = g.k;
         if (kind == 0) {
             if (k == 1) tile_dense<1>(smem, n, g, mats);
@@ -1738,9 +1741,11 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
         acc_first(a, x.rh, x.rl, x.rh, x.rl);
         acc_add(a, x.ih, x.il, x.ih, x.il);
         const ff r = acc_done(a);
-        probs[j] = ff2d(r.h, r.l);
+        const double pj = ff2d(r.h, r.l);   // prob_at's value for this amplitude
+        probs[j] = pj;
+        sprob[j] = pj;
     }
-    __syncthreads();   // the state just written is read back below (global writes of this CTA, visible after the barrier)
+    __syncthreads();
     if (shots <= 0) {
         small_run_done(done, ticket);
         return;
@@ -1748,14 +1753,13 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
     // The shots, as bs_sample draws them for a state of one CDF block (k_sample_small): the same
     // chunk sums and chunk prefix sums, the same in-chunk running sums (a warp's shuffle scan, kept
     // here per element), the same uniforms and comparisons, so the same indices; one thread per shot.
-    block_chunk_sums(psi, 0, nt, 0, s_ch, s_cl, &s_total, s_cinc);
+    block_chunk_sums_p(sprob, nt, 0, s_ch, s_cl, &s_total, s_cinc);
     double* scan = reinterpret_cast<double*>(smem);   // the tile is no longer needed
-    const int nc32 = (nt + kChunk - 1) / kChunk * kChunk;
     double* first = scan + nc32;                        // what a search compares in its first chunk
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int c = warp; c * kChunk < nt; c += nw) {
         const int i = c * kChunk + lane;
-        double p = (i < nt) ? prob_at(psi, 0, nt, i) : 0.0;
+        double p = (i < nt) ? sprob[i] : 0.0;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const double v = __shfl_up_sync(0xffffffffu, p, o);
@@ -1855,15 +1859,16 @@ int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dpr
                        "plan upload");
     bs_stage_done(s);
     if (rc) return rc;
-    // the tile, and afterwards two arrays of the sampler (whole 32-element chunks)
-    const size_t smem = std::max(((size_t)1 << n) * sizeof(float4), (size_t)2 * (((1 << n) + 31) / 32 * 32) * sizeof(double));
+    // the tile (afterwards two arrays of the sampler, whole 32-element chunks), then the probabilities
+    const size_t smem = std::max(((size_t)1 << n) * sizeof(float4), (size_t)2 * (((1 << n) + 31) / 32 * 32) * sizeof(double)) +
+                        ((size_t)1 << n) * sizeof(double);
     const TileGate* d_tg = (const TileGate*)dev;
     const float4* d_m = (const float4*)(dev + b_tg);
     const int32_t* d_p = (const int32_t*)(dev + b_tg + b_m);
     static bool attr_set[64] = {false};
     if (!attr_set[s->device & 63]) {
-        cudaFuncSetAttribute(k_small_run<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-        cudaFuncSetAttribute(k_small_run<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+        cudaFuncSetAttribute(k_small_run<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+        cudaFuncSetAttribute(k_small_run<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
         attr_set[s->device & 63] = true;
     }
     const int threads = std::min(512, std::max(128, (1 << n) / 2));
