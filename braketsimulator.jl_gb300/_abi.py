@@ -82,7 +82,9 @@ SIGNATURES = {
     "bs_dm_apply_vec_gate": (_i32, [_p, _P(_f64), _i32, _P(_i32), _i32, _P(_i32), _P(_i32), _u32]),
     "bs_apply_kraus": (_i32, [_p, _P(_f64), _i32, _i32, _P(_i32), _u32]),
     "bs_evolve": (_i32, [_p, _P(BsOp), _i64, _u32]),
-    "bs_run_small": (_i32, [_p, _P(BsOp), _i64, _i64, _u64, _P(_f64), _P(_i64)]),
+    # the output buffers as plain addresses (numpy's .ctypes.data): a typed-pointer conversion costs
+    # more than the rest of a small run's Python side
+    "bs_run_small": (_i32, [_p, _P(BsOp), _i64, _i64, _u64, _p, _p]),
     "bs_last_stats": (_i32, [_p, _P(BsStats)]),
     "bs_probabilities": (_i32, [_p, _P(_f64), _i64]),
     "bs_marginal_probabilities": (_i32, [_p, _i32, _P(_i32), _P(_f64)]),

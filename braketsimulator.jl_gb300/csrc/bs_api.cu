@@ -562,26 +562,32 @@ int bs_run_small(bs_sim* s, const bs_op* ops, int64_t n_ops, int64_t shots, uint
     s->defer_sync = defer;
     s->collect = nullptr;
     if (rc) return rc;
-    // mapped layout: the completion word (256 bytes), the probabilities, the shots
-    const size_t pb = ((size_t)dim * 8 + 255) & ~(size_t)255, sb = (size_t)shots * 8;
+    // mapped layout: the completion word and the kernel's start and end times (256 bytes), the
+    // probabilities, the shots, then room for the plan
+    const size_t pb = ((size_t)dim * 8 + 255) & ~(size_t)255, sb = ((size_t)shots * 8 + 255) & ~(size_t)255;
     const bool mapped = 256 + pb + sb <= kOutStage && map_stage();
     double* dprobs;
     int64_t* dsamp;
     int64_t* ddone = nullptr;
     int64_t ticket = 0;
+    SmallIO io{};
     if (mapped) {
         ddone = (int64_t*)t_map.d;
         ticket = ++t_map.ticket;
         dprobs = (double*)(t_map.d + 256);
         dsamp = (int64_t*)(t_map.d + 256 + pb);
+        io.hplan = t_map.h + 256 + pb + sb;
+        io.dplan = t_map.d + 256 + pb + sb;
+        io.plan_cap = kOutStage - (256 + pb + sb);
+        io.dtimes = (int64_t*)(t_map.d + 8);
     } else {
         rc = bs_ensure_scratch(s, (int64_t)(pb + sb) + 256);
         if (rc) return rc;
         dprobs = (double*)s->scratch;
         dsamp = (int64_t*)((char*)s->scratch + pb);
+        cudaEventRecord(s->ev0, s->stream);
     }
-    cudaEventRecord(s->ev0, s->stream);
-    rc = bs_run_small_sweeps(s, sweeps, dprobs, shots, seed, dsamp, ddone, ticket);
+    rc = bs_run_small_sweeps(s, sweeps, dprobs, shots, seed, dsamp, ddone, ticket, mapped ? &io : nullptr);
     if (rc == BS_ERR_UNSUPPORTED) {
         // a gate without an in-tile kernel (dense on more than 4 qubits) or a complex64 state: the usual
         // path, with the same results
@@ -593,8 +599,8 @@ int bs_run_small(bs_sim* s, const bs_op* ops, int64_t n_ops, int64_t shots, uint
     }
     if (rc) return rc;
     s->alias_valid = false;
-    cudaEventRecord(s->ev1, s->stream);
     if (!mapped) {
+        cudaEventRecord(s->ev1, s->stream);
         if (probs_out) cudaMemcpyAsync(probs_out, dprobs, (size_t)dim * 8, cudaMemcpyDeviceToHost, s->stream);
         if (sb) cudaMemcpyAsync(samples_out, dsamp, sb, cudaMemcpyDeviceToHost, s->stream);
         rc = bs_cuda_check(s, cudaStreamSynchronize(s->stream), "small run");
@@ -622,8 +628,11 @@ int bs_run_small(bs_sim* s, const bs_op* ops, int64_t n_ops, int64_t shots, uint
         if (rc) return rc;
     }
     if (probs_out) std::memcpy(probs_out, t_map.h + 256, (size_t)dim * 8);
-    if (sb) std::memcpy(samples_out, t_map.h + 256 + pb, sb);
-    s->stats_pending = true;   // the end event may still be on its way: bs_last_stats waits for it
+    if (shots > 0) std::memcpy(samples_out, t_map.h + 256 + pb, (size_t)shots * 8);
+    // device time: the kernel's own start and end stamps (no events on this path)
+    const volatile int64_t* times = reinterpret_cast<const volatile int64_t*>(t_map.h + 8);
+    s->stats.gpu_ms = (double)(times[1] - times[0]) * 1e-6;
+    s->stats_pending = false;
     return BS_OK;
 }
 

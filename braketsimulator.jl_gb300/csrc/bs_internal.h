@@ -188,6 +188,14 @@ int bs_alias_parallel(bs_sim* s, const double* dprobs, int64_t n, double wsum, d
 // addresses, mapped host memory included); at its end the kernel writes `ticket` into *done (a
 // host-mapped word, may be null) once every result is visible to the host.  BS_ERR_UNSUPPORTED
 // (nothing launched) when a gate has no in-tile kernel or the state is not a complex128 state vector
-// of at most 12 qubits.
+// of at most 12 qubits.  io (may be null): host-mapped memory for the plan (written at hplan, read by
+// the kernel at dplan, when it fits in plan_cap bytes; otherwise the plan is uploaded) and for the
+// kernel's start and end times (globaltimer nanoseconds, at dtimes[0] and dtimes[1]).
+struct SmallIO {
+    char* hplan;
+    char* dplan;
+    size_t plan_cap;
+    int64_t* dtimes;
+};
 int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dprobs, int64_t shots, uint64_t seed,
-                        int64_t* dsamples, int64_t* done, int64_t ticket);
+                        int64_t* dsamples, int64_t* done, int64_t ticket, const SmallIO* io);

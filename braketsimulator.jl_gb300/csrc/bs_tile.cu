@@ -9,6 +9,7 @@
 // kernels src/custom_gates.jl:364-416; the density-matrix gate of
 // src/dm_simulator.jl:130-140 is two tile gates (column bits U, row bits conj U).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -47,8 +48,15 @@ __device__ __forceinline__ void stage_gates(TileGate* dst, const TileGate* __res
 __device__ __forceinline__ cff f4c(float4 v) { return {v.x, v.z, v.y, v.w}; }
 __device__ __forceinline__ float4 c4f(const cff& c) { return make_float4(c.rh, c.ih, c.rl, c.il); }
 __device__ __forceinline__ cff f4m(float4 v) { return {v.x, v.y, v.z, v.w}; }
+// read-only operand load: through the non-coherent cache from global memory, or plainly from shared
+// memory (operands staged there)
+template <bool S, typename V>
+__device__ __forceinline__ V ldro(const V* p) {
+    if constexpr (S) return *p;
+    else return __ldg(p);
+}
 
-template <int K, bool SW = false>
+template <int K, bool SW = false, bool SM = false>
 __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* __restrict__ mats) {
     constexpr int D = 1 << K;
     int pos[K];
@@ -68,7 +76,7 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
     for (int q = 0; q < K; q++) tb[q] = g.tbit[q];
     if (K == 1) {
         // 2x2: matrix held in registers across the thread's pairs
-        const cff m00 = f4m(__ldg(m)), m01 = f4m(__ldg(m + 1)), m10 = f4m(__ldg(m + 2)), m11 = f4m(__ldg(m + 3));
+        const cff m00 = f4m(ldro<SM>(m)), m01 = f4m(ldro<SM>(m + 1)), m10 = f4m(ldro<SM>(m + 2)), m11 = f4m(ldro<SM>(m + 3));
         const int b0 = 1 << tb[0];
 #pragma unroll 2
         for (int gr = threadIdx.x; gr < ngroups; gr += blockDim.x) {
@@ -105,16 +113,16 @@ __device__ void tile_dense(float4* sm, int T, const TileGate& g, const float4* _
 #pragma unroll
         for (int r = 0; r < D; r++) {
             ffacc ar, ai;
-            cmac_first(ar, ai, f4m(__ldg(m + r * D)), x[0]);
+            cmac_first(ar, ai, f4m(ldro<SM>(m + r * D)), x[0]);
 #pragma unroll
-            for (int c = 1; c < D; c++) cmac(ar, ai, f4m(__ldg(m + r * D + c)), x[c]);
+            for (int c = 1; c < D; c++) cmac(ar, ai, f4m(ldro<SM>(m + r * D + c)), x[c]);
             sm[idx[r]] = c4f(cdone(ar, ai));
         }
     }
 }
 
 // monomial gate: column c goes to row perm[2c] with phase i^perm[2c+1]
-template <int K, bool SW = false>
+template <int K, bool SW = false, bool SM = false>
 __device__ void tile_monomial(float4* sm, int T, const TileGate& g, const int32_t* __restrict__ perms) {
     constexpr int D = 1 << K;
     int pos[K];
@@ -144,7 +152,7 @@ __device__ void tile_monomial(float4* sm, int T, const TileGate& g, const int32_
         }
 #pragma unroll
         for (int c = 0; c < D; c++) {
-            const int r = __ldg(p + 2 * c), ph = __ldg(p + 2 * c + 1);
+            const int r = ldro<SM>(p + 2 * c), ph = ldro<SM>(p + 2 * c + 1);
             int j = jb;
 #pragma unroll
             for (int q = 0; q < K; q++) if ((r >> q) & 1) j |= 1 << g.tbit[q];
@@ -162,7 +170,7 @@ __device__ __forceinline__ bool parity_odd(const TileGate& g, int64_t gi) {
 }
 
 // off_tab[h] << osh: global offset of the tile's high-bit pattern h
-template <typename OT, bool SW = false>
+template <typename OT, bool SW = false, bool SM = false>
 __device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const float4* __restrict__ mats,
                           int64_t base, OT off_tab, int osh) {
     const int nt = 1 << T, lowmask = (1 << L) - 1;
@@ -190,7 +198,7 @@ __device__ void tile_diag(float4* sm, int T, int L, const TileGate& g, const flo
             const int64_t gi = base | ((int64_t)off_tab[j >> L] << osh) | (int64_t)(j & lowmask);
             for (int q = 0; q < g.k; q++) di |= (int)((gi >> g.gbit[q]) & 1) << q;
         }
-        float4 d = __ldg(m + di);
+        float4 d = ldro<SM>(m + di);
         if (d.y == 0.f && d.w == 0.f) {
             if (d.z == 0.f && d.x == 1.f) continue;
             if (d.z == 0.f && d.x == -1.f) { sm[js] = c4f(cmul_ipow(f4c(sm[js]), 2)); continue; }
@@ -1690,46 +1698,69 @@ struct NoOff {
     __device__ __forceinline__ int64_t operator[](int) const { return 0; }
 };
 
-// The end of a small run, for a host that polls instead of synchronising: every thread's writes are
-// made visible to the system, then one thread writes the call's ticket into the host-mapped word.
-__device__ __forceinline__ void small_run_done(volatile int64_t* done, int64_t ticket) {
+__device__ __forceinline__ int64_t globaltimer_ns() {
+    int64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// The end of a small run, for a host that polls instead of synchronising: the kernel's end time, then
+// every thread's writes are made visible to the system, then one thread writes the call's ticket into
+// the host-mapped word.
+__device__ __forceinline__ void small_run_done(volatile int64_t* done, int64_t ticket, int64_t* times) {
     if (!done) return;
+    if (times && threadIdx.x == 0) times[1] = globaltimer_ns();
     __threadfence_system();
     __syncthreads();
     if (threadIdx.x == 0) *done = ticket;
 }
 
-template <int KMAX>
+// STAGED: the matrices and permutations are copied into shared memory first (one round trip to the
+// plan, which may live in host-mapped memory) instead of being read from the plan at every gate.
+template <int KMAX, bool STAGED>
 __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, int n, const TileGate* __restrict__ gates,
-                                                   int ng, const float4* __restrict__ mats,
-                                                   const int32_t* __restrict__ perms, double* __restrict__ probs,
-                                                   int64_t shots, uint64_t seed, int64_t* __restrict__ samples,
-                                                   volatile int64_t* done, int64_t ticket) {
+                                                   int ng, const float4* __restrict__ mats, int n_mats,
+                                                   const int32_t* __restrict__ perms, int n_perms,
+                                                   double* __restrict__ probs, int64_t shots, uint64_t seed,
+                                                   int64_t* __restrict__ samples, volatile int64_t* done, int64_t ticket,
+                                                   int64_t* times) {
+    if (times && threadIdx.x == 0) times[0] = globaltimer_ns();
     extern __shared__ float4 smem[];
     __shared__ float s_ch[kCpb], s_cl[kCpb];
     __shared__ double s_cinc[kCpb], s_total;
     __shared__ long long s_ckey[kCpb];
     __shared__ TileGate s_gates[kGateChunk];
     const int nt = 1 << n, nc32 = (nt + kChunk - 1) / kChunk * kChunk;
-    // the probabilities, after the tile (or after the sampler's two arrays, which replace the tile)
+    // the probabilities, after the tile (or after the sampler's two arrays, which replace the tile),
+    // then the staged matrices and permutations
     double* sprob = reinterpret_cast<double*>(reinterpret_cast<char*>(smem) + max(nt * 16, 2 * nc32 * 8));
+    const float4* m_op = mats;
+    const int32_t* p_op = perms;
+    if (STAGED) {
+        float4* ms = reinterpret_cast<float4*>(sprob + nt);
+        int32_t* ps = reinterpret_cast<int32_t*>(ms + n_mats);
+        for (int j = threadIdx.x; j < n_mats; j += blockDim.x) ms[j] = mats[j];
+        for (int j = threadIdx.x; j < n_perms; j += blockDim.x) ps[j] = perms[j];
+        m_op = ms;
+        p_op = ps;   // read after the barrier that opens the first chunk of gates
+    }
     for (int j = threadIdx.x; j < nt; j += blockDim.x) smem[j] = make_float4(j == 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
     for (int gi = 0; gi < ng; gi++) {
         if (gi % kGateChunk == 0) stage_gates(s_gates, gates + gi, min(kGateChunk, ng - gi));   // one latency per 32 gates
         const TileGate& g = s_gates[gi % kGateChunk];
         const int kind = g.kind, k = g.k;
         if (kind == 0) {
-            if (k == 1) tile_dense<1>(smem, n, g, mats);
-            else if (k == 2) tile_dense<2>(smem, n, g, mats);
-            else if (KMAX == 4 && k == 3) tile_dense<3>(smem, n, g, mats);
-            else if (KMAX == 4) tile_dense<4>(smem, n, g, mats);
+            if (k == 1) tile_dense<1, false, STAGED>(smem, n, g, m_op);
+            else if (k == 2) tile_dense<2, false, STAGED>(smem, n, g, m_op);
+            else if (KMAX == 4 && k == 3) tile_dense<3, false, STAGED>(smem, n, g, m_op);
+            else if (KMAX == 4) tile_dense<4, false, STAGED>(smem, n, g, m_op);
         } else if (kind == 1) {
-            tile_diag<NoOff>(smem, n, n, g, mats, 0, NoOff{}, 0);
+            tile_diag<NoOff, false, STAGED>(smem, n, n, g, m_op, 0, NoOff{}, 0);
         } else {
-            if (k == 1) tile_monomial<1>(smem, n, g, perms);
-            else if (k == 2) tile_monomial<2>(smem, n, g, perms);
-            else if (KMAX == 4 && k == 3) tile_monomial<3>(smem, n, g, perms);
-            else if (KMAX == 4) tile_monomial<4>(smem, n, g, perms);
+            if (k == 1) tile_monomial<1, false, STAGED>(smem, n, g, p_op);
+            else if (k == 2) tile_monomial<2, false, STAGED>(smem, n, g, p_op);
+            else if (KMAX == 4 && k == 3) tile_monomial<3, false, STAGED>(smem, n, g, p_op);
+            else if (KMAX == 4) tile_monomial<4, false, STAGED>(smem, n, g, p_op);
         }
         __syncthreads();
     }
@@ -1747,7 +1778,7 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
     }
     __syncthreads();
     if (shots <= 0) {
-        small_run_done(done, ticket);
+        small_run_done(done, ticket, times);
         return;
     }
     // The shots, as bs_sample draws them for a state of one CDF block (k_sample_small): the same
@@ -1755,18 +1786,33 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
     // here per element), the same uniforms and comparisons, so the same indices; one thread per shot.
     block_chunk_sums_p(sprob, nt, 0, s_ch, s_cl, &s_total, s_cinc);
     double* scan = reinterpret_cast<double*>(smem);   // the tile is no longer needed
-    double* first = scan + nc32;                        // what a search compares in its first chunk
+    // per element: the largest value, as an integer key, of (chunk base + running sum) over the chunk
+    // up to it, so that a binary search finds the first element whose own value reaches the target
+    long long* fkey = reinterpret_cast<long long*>(scan + nc32);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int c = warp; c * kChunk < nt; c += nw) {
         const int i = c * kChunk + lane;
         double p = (i < nt) ? sprob[i] : 0.0;
+        const double cb = c == 0 ? 0.0 : s_cinc[c - 1];   // 0.0 + cb is cb: the sums are non-negative
+        if (__ballot_sync(0xffffffffu, p != 0.0) == 0u) {
+            // a chunk of zeros: every running sum is 0, every compared value the chunk base
+            scan[i] = 0.0;
+            fkey[i] = __double_as_longlong(cb);
+            continue;
+        }
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const double v = __shfl_up_sync(0xffffffffu, p, o);
             if (lane >= o) p += v;
         }
         scan[i] = p;
-        first[i] = (0.0 + (c == 0 ? 0.0 : s_cinc[c - 1])) + p;
+        long long key = __double_as_longlong(cb + p);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long v = __shfl_up_sync(0xffffffffu, key, o);
+            if (lane >= o) key = max(key, v);
+        }
+        fkey[i] = key;
     }
     for (int c = threadIdx.x; c < kCpb; c += blockDim.x) s_ckey[c] = __double_as_longlong(0.0 + s_cinc[c]);
     __syncthreads();
@@ -1782,11 +1828,15 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
             const int mid = (clo + chi) >> 1;
             if (s_ckey[mid] >= tb) chi = mid; else clo = mid + 1;
         }
-        int64_t out = nt - 1;
-        bool found = false;
         const int c0 = clo * kChunk;
-        for (int l = 0; l < kChunk && c0 + l < nt; l++)
-            if (__double_as_longlong(first[c0 + l]) >= tb) { out = c0 + l; found = true; break; }
+        int lo = 0, hi = kChunk;   // first element of the chunk whose value reaches the target
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (fkey[c0 + mid] >= tb) hi = mid; else lo = mid + 1;
+        }
+        int64_t out = nt - 1;
+        bool found = lo < kChunk && c0 + lo < nt;
+        if (found) out = c0 + lo;
         if (!found && c0 < nt) {
             // the chunk's own running sum fell short of its prefix sum by rounding: go on as the
             // one-block sampler does, with the running sum carried from chunk to chunk
@@ -1801,13 +1851,13 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
         }
         samples[sh] = out;
     }
-    small_run_done(done, ticket);
+    small_run_done(done, ticket, times);
 }
 
 }  // namespace
 
 int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dprobs, int64_t shots, uint64_t seed,
-                        int64_t* dsamples, int64_t* done, int64_t ticket) {
+                        int64_t* dsamples, int64_t* done, int64_t ticket, const SmallIO* io) {
     const int n = s->n;
     if (s->kind != BS_KIND_SV || s->precision != BS_PREC_C128 || n > 12) return BS_ERR_UNSUPPORTED;
     std::vector<TileGate> tg;
@@ -1847,37 +1897,57 @@ int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dpr
     const int64_t b_tg = al((int64_t)(tg.size() + 1) * (int64_t)sizeof(TileGate));
     const int64_t b_m = al((int64_t)(mats.size() + 1) * (int64_t)sizeof(float4));
     const int64_t b_p = al((int64_t)(perms.size() + 1) * (int64_t)sizeof(int32_t));
-    int rc = bs_ensure_plan(s, b_tg + b_m + b_p);
-    if (rc) return rc;
-    char* host = bs_stage(s, (size_t)(b_tg + b_m + b_p));
-    if (!host) return bs_fail(s, BS_ERR_ALLOC, "pinned staging allocation");
-    if (!tg.empty()) std::memcpy(host, tg.data(), tg.size() * sizeof(TileGate));
-    if (!mats.empty()) std::memcpy(host + b_tg, mats.data(), mats.size() * sizeof(float4));
-    if (!perms.empty()) std::memcpy(host + b_tg + b_m, perms.data(), perms.size() * sizeof(int32_t));
-    char* dev = (char*)s->plan_buf;
-    rc = bs_cuda_check(s, cudaMemcpyAsync(dev, host, (size_t)(b_tg + b_m + b_p), cudaMemcpyHostToDevice, s->stream),
-                       "plan upload");
-    bs_stage_done(s);
-    if (rc) return rc;
-    // the tile (afterwards two arrays of the sampler, whole 32-element chunks), then the probabilities
-    const size_t smem = std::max(((size_t)1 << n) * sizeof(float4), (size_t)2 * (((1 << n) + 31) / 32 * 32) * sizeof(double)) +
+    const int64_t b_all = b_tg + b_m + b_p;
+    char* dev;
+    int rc;
+    if (io && b_all <= (int64_t)io->plan_cap) {
+        // the plan goes straight into host-mapped memory, which the kernel reads (the previous run on
+        // this thread has completed, so nothing reads it any more); the launch orders these writes
+        // before the kernel's reads
+        char* host = io->hplan;
+        if (!tg.empty()) std::memcpy(host, tg.data(), tg.size() * sizeof(TileGate));
+        if (!mats.empty()) std::memcpy(host + b_tg, mats.data(), mats.size() * sizeof(float4));
+        if (!perms.empty()) std::memcpy(host + b_tg + b_m, perms.data(), perms.size() * sizeof(int32_t));
+        std::atomic_thread_fence(std::memory_order_release);
+        dev = io->dplan;
+    } else {
+        rc = bs_ensure_plan(s, b_all);
+        if (rc) return rc;
+        char* host = bs_stage(s, (size_t)b_all);
+        if (!host) return bs_fail(s, BS_ERR_ALLOC, "pinned staging allocation");
+        if (!tg.empty()) std::memcpy(host, tg.data(), tg.size() * sizeof(TileGate));
+        if (!mats.empty()) std::memcpy(host + b_tg, mats.data(), mats.size() * sizeof(float4));
+        if (!perms.empty()) std::memcpy(host + b_tg + b_m, perms.data(), perms.size() * sizeof(int32_t));
+        dev = (char*)s->plan_buf;
+        rc = bs_cuda_check(s, cudaMemcpyAsync(dev, host, (size_t)b_all, cudaMemcpyHostToDevice, s->stream), "plan upload");
+        bs_stage_done(s);
+        if (rc) return rc;
+    }
+    // the tile (afterwards two arrays of the sampler, whole 32-element chunks), then the probabilities,
+    // then (staged) the matrices and permutations
+    const size_t base = std::max(((size_t)1 << n) * sizeof(float4), (size_t)2 * (((1 << n) + 31) / 32 * 32) * sizeof(double)) +
                         ((size_t)1 << n) * sizeof(double);
+    const size_t stage = mats.size() * sizeof(float4) + perms.size() * sizeof(int32_t);
+    constexpr size_t kSmemCap = 160 * 1024;
+    const bool staged = base + stage <= kSmemCap;
+    const size_t smem = staged ? base + stage : base;
     const TileGate* d_tg = (const TileGate*)dev;
     const float4* d_m = (const float4*)(dev + b_tg);
     const int32_t* d_p = (const int32_t*)(dev + b_tg + b_m);
     static bool attr_set[64] = {false};
     if (!attr_set[s->device & 63]) {
-        cudaFuncSetAttribute(k_small_run<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-        cudaFuncSetAttribute(k_small_run<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+        cudaFuncSetAttribute(k_small_run<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap);
+        cudaFuncSetAttribute(k_small_run<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap);
+        cudaFuncSetAttribute(k_small_run<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap);
+        cudaFuncSetAttribute(k_small_run<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemCap);
         attr_set[s->device & 63] = true;
     }
     const int threads = std::min(512, std::max(128, (1 << n) / 2));
-    if (kmax <= 2)
-        k_small_run<2><<<1, threads, smem, s->stream>>>((double2*)s->state, n, d_tg, (int)tg.size(), d_m, d_p, dprobs,
-                                                        shots, seed, dsamples, done, ticket);
-    else
-        k_small_run<4><<<1, threads, smem, s->stream>>>((double2*)s->state, n, d_tg, (int)tg.size(), d_m, d_p, dprobs,
-                                                        shots, seed, dsamples, done, ticket);
+    auto kern = kmax <= 2 ? (staged ? k_small_run<2, true> : k_small_run<2, false>)
+                          : (staged ? k_small_run<4, true> : k_small_run<4, false>);
+    kern<<<1, threads, smem, s->stream>>>((double2*)s->state, n, d_tg, (int)tg.size(), d_m, (int)mats.size(), d_p,
+                                          (int)perms.size(), dprobs, shots, seed, dsamples, done, ticket,
+                                          io ? io->dtimes : nullptr);
     s->stats.kernel_launches++;
     s->stats.sweeps++;
     s->stats.gates += (int64_t)tg.size();

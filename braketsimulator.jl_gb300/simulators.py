@@ -44,9 +44,19 @@ def _ops_for(instructions, dm: bool, noise_mode: int):
     ops = []    # the bs_op structs as bytes, joined into one array below
     keep = []
     skip = (Measure, Reset, Barrier, Delay)
+    cache = _LOWER_CACHE
     for ix in instructions:
         op = ix.operator
         t = ix.target
+        tp = type(op)
+        if tp in _BY_VALUE:
+            # a fixed gate lowered before (the common case of repeated circuits): no dispatch
+            hit = cache.get((tp, op.angle, op.pow_exponent, t))
+            if hit is not None:
+                for o, buf in hit:
+                    ops.append(o)
+                    keep.append(buf)
+                continue
         if isinstance(op, skip):
             continue
         if isinstance(op, Noise):
@@ -88,6 +98,9 @@ _LOWER_CACHE_MAX = 1 << 16
 _BSOP_SIZE = C.sizeof(_abi.BsOp)
 _OFF_NT, _OFF_T0, _OFF_MAT = _abi.BsOp.n_targets.offset, _abi.BsOp.targets.offset, _abi.BsOp.matrix.offset
 _ROTATIONS = (Rx, Ry, Rz)
+# gate types whose lowering is cached by value (type, angles, pow_exponent, targets): every Gate
+# type but the matrix-carrying ones (Unitary, Control), added as they are first lowered
+_BY_VALUE = set()
 
 
 def _rotation_op(op, q: int):
@@ -108,6 +121,7 @@ def _gate_ops(op, t):
         return _rotation_op(op, t[0])
     key = None
     if not isinstance(op, (Unitary, Control)):
+        _BY_VALUE.add(type(op))
         key = (type(op), op.angle, op.pow_exponent, t)
         hit = _LOWER_CACHE.get(key)
         if hit is not None:
@@ -360,7 +374,7 @@ class StateVectorSimulator(AbstractSimulator):
         p = np.empty(1 << self.qubit_count, dtype=np.float64) if probabilities else None
         smp = np.empty(shots, dtype=np.int64)
         self._h.call("bs_run_small", arr, n_ops, shots, C.c_uint64(seed & 0xFFFFFFFFFFFFFFFF),
-                     _abi.dptr(p) if p is not None else None, _abi.i64ptr(smp))
+                     p.ctypes.data if p is not None else None, smp.ctypes.data)
         del keep
         self._obs = None
         return p, smp
