@@ -1819,9 +1819,12 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
     // Every value compared below is a sum of probabilities, so non-negative: its order is the order of
     // its bit pattern as an integer, which keeps the comparisons off the FP64 pipe (2 per clock per SM).
     const double total = 0.0 + s_total;
+    // u * total with u = (r >> 11) 2^-53: the scaling by 2^-53 is exact on either factor, so
+    // (r >> 11) * (total 2^-53) rounds the same real product once, as the samplers' u * total does
+    const double tscale = total * 0x1.0p-53;
     for (int64_t sh = threadIdx.x; sh < shots; sh += blockDim.x) {
         const uint64_t r = splitmix64(seed ^ splitmix64((uint64_t)sh));
-        const double t = (double)(r >> 11) * 0x1.0p-53 * total;
+        const double t = (double)(r >> 11) * tscale;
         const long long tb = __double_as_longlong(t);
         int clo = 0, chi = kCpb - 1;
         while (clo < chi) {
@@ -1864,8 +1867,8 @@ int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dpr
     std::vector<float4> mats;
     std::vector<int32_t> perms;
     int kmax = 1;
+    std::vector<HostGate> merged;
     for (const Sweep& sw : sweeps) {
-        std::vector<HostGate> merged;
         merge_diagonals(sw.gates, merged);
         for (const HostGate& hg : merged) {
             if (hg.kind != 0 && hg.kind != 1 && hg.kind != 2) return BS_ERR_UNSUPPORTED;

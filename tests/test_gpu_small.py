@@ -45,6 +45,41 @@ def test_run_random_circuits(n, pows):
     assert np.all(np.abs(ref[s]) ** 2 > 1e-14)
 
 
+@pytest.mark.parametrize("n", [4, 9, 12])
+def test_run_permutation_heavy_circuits(n):
+    """Long runs of permutation gates (CNOT chains, SWAPs, X, Y, CCNOT, controlled Y and their mixes)
+    after a dense layer: the state must be the usual path's, since such gates only move and negate
+    values, and the oracle's to 1e-12."""
+    rng = np.random.default_rng(40 + n)
+    ops = [bs.Instruction(bs.H(), [q]) for q in range(n)] + [bs.Instruction(bs.Ry(0.3 + 0.1 * q), [q]) for q in range(n)]
+    for _ in range(60):
+        qs = [int(x) for x in rng.choice(n, min(3, n), replace=False)]
+        r = int(rng.integers(7))
+        if r == 0:
+            ops.append(bs.Instruction(bs.CNot(), qs[:2]))
+        elif r == 1:
+            ops.append(bs.Instruction(bs.Swap(), qs[:2]))
+        elif r == 2:
+            ops.append(bs.Instruction(bs.X(), qs[:1]))
+        elif r == 3:
+            ops.append(bs.Instruction(bs.Y(), qs[:1]))
+        elif r == 4 and n >= 3:
+            ops.append(bs.Instruction(bs.CCNot(), qs[:3]))
+        elif r == 5:
+            ops.append(bs.Instruction(bs.CY(), qs[:2]))
+        else:
+            ops.append(bs.Instruction(bs.CNot(), [qs[0], (qs[0] + 1) % n]))
+    sim = bs.StateVectorSimulator(n, 400)
+    p, s = sim.run(ops, 400, seed=4)
+    usual = bs.StateVectorSimulator(n, 400).evolve(ops)
+    assert rel_err(sim.state_vector, usual.state_vector) < 1e-15
+    assert rel_err(p, usual.probabilities()) < 1e-15
+    assert np.array_equal(sim.samples(4), s)     # the same draws from the state the run left
+    ref = oracle.OracleSV(n).evolve(ops).psi
+    assert rel_err(sim.state_vector, ref) < 1e-12
+    assert np.all(np.abs(ref[s]) ** 2 > 1e-14)
+
+
 def test_run_repeats_and_resets():
     """Each call starts from |0...0> whatever the handle held; the same seed gives the same shots."""
     ops = ghz(6) + [bs.Instruction(bs.Ry(0.4), [3])]
