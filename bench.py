@@ -455,7 +455,11 @@ def ghz_bench(bs, reps=2000, cpu=False):
         p4 = sim.probabilities()
         s4 = sim.samples(r)
     dt4 = (time.perf_counter() - t0) / (reps // 4)
-    ok = ok and np.array_equal(p4, p) and np.array_equal(s4, s)
+    # both flows give the same probabilities and, for the same seed, the same shots
+    p, s = sim.run(ops, 1000, seed=reps)
+    sim.reinit(10, 1000)
+    sim.evolve(ops)
+    ok = ok and np.array_equal(sim.probabilities(), p) and np.array_equal(sim.samples(reps), s)
     out = {"us_per_circuit": round(dt * 1e6, 1), "circuits_per_s": round(1 / dt, 1),
            "api": "StateVectorSimulator.run (bs_run_small)", "four_calls_us_per_circuit": round(dt4 * 1e6, 1),
            "checked": bool(ok)}
@@ -628,7 +632,14 @@ def batch_bench(bs, cpu=False):
     t_rep = (time.perf_counter() - t0) / reps
     same = bool(np.array_equal(exp, exp2))
     cb.close()
+    hbm, _, src = peaks()
+    # the batch's roofline: the sweeps' algorithmic bytes (one read and one write of a circuit's state
+    # per sweep, 8 B per complex64 amplitude) over the batch's device time, against the HBM copy rate
+    gbps = st2["bytes_moved"] / (st2["gpu_ms"] * 1e-3) / 1e9 if st2["gpu_ms"] > 0 else None
+    roof = {"sweep_bytes": st2["bytes_moved"], "executed_sweep_GBps": round(gbps, 1) if gbps else None,
+            "hbm_frac": round(gbps / hbm, 3) if gbps else None, "peak_GBps": hbm, "peak_source": src}
     return {"circuits": len(circuits), "qubits": "12..26", "gates": int(sum(len(c) for c in circuits)),
+            "roofline": roof,
             "shots_each": 1000, "expectations_each": 8, "precision": "c64 (FP64 reductions)",
             "s_per_batch": round(dt, 3), "circuits_per_s": round(len(circuits) / dt, 1),
             "device_ms": round(st["gpu_ms"], 1), "sweeps": st["sweeps"],
