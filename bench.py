@@ -811,6 +811,14 @@ def _only_batch_small(bs):
     return {"circuits": len(keep)}
 
 
+def _only_ghz(bs):
+    ops = [bs.Instruction(bs.H(), [0])] + [bs.Instruction(bs.CNot(), [0, k]) for k in range(1, 10)]
+    sim = bs.StateVectorSimulator(10, 1000)
+    for r in range(50):
+        sim.run(ops, 1000, seed=r)
+    return {"kernel_us": sim.last_stats()["gpu_ms"] * 1e3}
+
+
 def _only_dense(bs):
     n = 27
     sim = bs.StateVectorSimulator(n, 0)
@@ -828,6 +836,7 @@ PROFILE_WORKLOADS = {
     "sample26": (_only_sample, "k_block_sums / k_sample_rng: 1e5 shots of a 26-qubit state"),
     "batch_small": (_only_batch_small, "k_batch_small: the <= 12-qubit circuits of a 256-circuit batch"),
     "dense27": (_only_dense, "k_tile_sweep_tc: the dense circuit at 27 qubits (2 GiB state)"),
+    "ghz10": (_only_ghz, "k_small_run: GHZ-10 with 1000 shots through StateVectorSimulator.run, 50 times"),
 }
 
 

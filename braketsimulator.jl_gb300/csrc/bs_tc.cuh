@@ -318,11 +318,13 @@ __device__ __forceinline__ bool wait_bar1(const State& st, int k) {
 // gnext: the tile's next fused gate, whose digit slices are copied ahead as soon as this gate's
 // MMAs have completed (null: none, or it copies its own); s_nsrc: shared scratch for their source.
 // The swizzle is linear over XOR, so the position of column m's amplitude t is
-// sw(column bits) ^ sw(target bits of t).
+// sw(column bits) ^ sw(target bits of t); both come from the gate's host-made table (tab: 56
+// uint16, sw of the column bits of m & 15 and of m >> 4, then sw of the target bits of t).
 // On a wait that gives up, sets *fail and *err and leaves the tile partly updated.
 template <int NT>
 __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const TileGate* gnext,
-                                      const uint16_t* __restrict__ pool, uint16_t* sB, State& st, int64_t base,
+                                      const uint16_t* __restrict__ pool, const uint16_t* __restrict__ tab,
+                                      uint16_t* sB, State& st, int64_t base,
                                       uint32_t* s_wmax, bool emax_ok, int* s_tsw, const uint16_t** s_nsrc, int* s_fail,
                                       int* err) {
     constexpr int HP = NT / 128;   // threads per column
@@ -330,20 +332,8 @@ __device__ __forceinline__ void apply(float4* sm, const TileGate& g, const TileG
     const int tid = threadIdx.x, warp = tid >> 5, lane_id = tid & 31, m = tid & 127, h = tid >> 7;
     // the previous readers of sB (the MMAs of the previous fused gate) have completed
     if (!st.pref && tid == 0) copy_slices(su32(sB), slice_src(g, pool, base), st.bar);
-    int tb[5];
-    uint32_t tmask = 0;
-#pragma unroll
-    for (int q = 0; q < 5; q++) { tb[q] = g.gbit[q]; tmask |= 1u << tb[q]; }
-    if (tid < 32) {
-        int p = 0;
-#pragma unroll
-        for (int q = 0; q < 5; q++) if ((tid >> q) & 1) p |= 1 << tb[q];
-        s_tsw[tid] = sw(p);
-    }
-    int pm = 0;
-    for (int b = 0, src = 0; b < 12; b++)
-        if (!((tmask >> b) & 1u)) { pm |= ((m >> src) & 1) << b; src++; }
-    const int spm = sw(pm);
+    if (tid < 32) s_tsw[tid] = tab[24 + tid];
+    const int spm = tab[m & 15] ^ tab[16 + (m >> 4)];
     const int* tsw = s_tsw + NA * h;
     // Tile scale: the largest exponent of the high words over the tile, per warp in s_wmax.  It was
     // left there by the previous fused gate's write-back or the tile load unless a gate that may

@@ -506,7 +506,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_sweep_tc(double2* __rest
                 have = true;
             }
             const TileGate* gn = q + 1 < s_ntc ? d.gates + s_tcq[q + 1] : nullptr;
-            tc::apply<kTcThreads>(smem, g, gn, d.tc_pool, sB, st, base, s_wmax, emax_ok, s_tsw, &s_nsrc, &s_fail,
+            tc::apply<kTcThreads>(smem, g, gn, d.tc_pool, reinterpret_cast<const uint16_t*>(d.perms + g.perm_off), sB,
+                                  st, base, s_wmax, emax_ok, s_tsw, &s_nsrc, &s_fail,
                                   d.err);
             q++;
             emax_ok = true;
@@ -1247,6 +1248,38 @@ void merge_diagonals(const std::vector<HostGate>& in, std::vector<HostGate>& out
 
 }  // namespace
 
+namespace {
+// The tensor-core sweep's offsets of a fused gate on tile bits tb[0..4], in its bank-swizzled tile
+// (tc::sw, restated here for the host): 56 uint16 packed two per int32 — sw of the deposit of a
+// column index's bits 0..3 and 4..6 into the 7 other tile bits (ascending), then sw of each of the 32
+// target patterns.  The swizzle is linear over XOR, so sw(column) = table[m & 15] ^ table[16 + (m >> 4)].
+int host_sw(int j) { return j ^ (((j >> 3) ^ (j >> 6) ^ (j >> 9)) & 7); }
+void tc_offset_tables(const int32_t* tb, std::vector<int32_t>& out) {
+    uint32_t tmask = 0;
+    for (int q = 0; q < 5; q++) tmask |= 1u << tb[q];
+    int nb[7], k = 0;
+    for (int b = 0; b < 12; b++)
+        if (!((tmask >> b) & 1u)) nb[k++] = b;
+    uint16_t v[56];
+    for (int i = 0; i < 16; i++) {
+        int p = 0;
+        for (int j = 0; j < 4; j++) if ((i >> j) & 1) p |= 1 << nb[j];
+        v[i] = (uint16_t)host_sw(p);
+    }
+    for (int i = 0; i < 8; i++) {
+        int p = 0;
+        for (int j = 0; j < 3; j++) if ((i >> j) & 1) p |= 1 << nb[4 + j];
+        v[16 + i] = (uint16_t)host_sw(p);
+    }
+    for (int t = 0; t < 32; t++) {
+        int p = 0;
+        for (int q = 0; q < 5; q++) if ((t >> q) & 1) p |= 1 << tb[q];
+        v[24 + t] = (uint16_t)host_sw(p);
+    }
+    for (int i = 0; i < 28; i++) out.push_back((int32_t)((uint32_t)v[2 * i] | ((uint32_t)v[2 * i + 1] << 16)));
+}
+}  // namespace
+
 int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     if (sweeps.empty()) return BS_OK;
     const int n_bits = bs_vec_bits(s);
@@ -1357,6 +1390,8 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
                 t.kind = 4;
                 t.k = 5;
                 for (int q = 0; q < 5; q++) t.gbit[q] = local[hg.ebit[q]];
+                t.perm_off = (int32_t)perms.size();
+                tc_offset_tables(t.gbit, perms);
                 const int nvar = 1 << hg.ubits.size();
                 t.tc_nu = (int32_t)hg.ubits.size();
                 for (size_t i = 0; i < hg.ubits.size(); i++) t.tc_ub[i] = hg.ubits[i];
