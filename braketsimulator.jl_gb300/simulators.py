@@ -39,6 +39,11 @@ class Instruction:
         return f"Instruction({self.operator!r}, {list(self.target)})"
 
 
+def _addr(a: np.ndarray) -> int:
+    """Address of a writable contiguous array's data (cheaper than ``a.ctypes.data``)."""
+    return C.addressof(C.c_char.from_buffer(a)) if a.size else a.ctypes.data
+
+
 def _ops_for(instructions, dm: bool, noise_mode: int):
     """Lower instructions into a bs_op array; returns (array, keepalive buffers)."""
     ops = []    # the bs_op structs as bytes, joined into one array below
@@ -374,7 +379,7 @@ class StateVectorSimulator(AbstractSimulator):
         p = np.empty(1 << self.qubit_count, dtype=np.float64) if probabilities else None
         smp = np.empty(shots, dtype=np.int64)
         self._h.call("bs_run_small", arr, n_ops, shots, C.c_uint64(seed & 0xFFFFFFFFFFFFFFFF),
-                     p.ctypes.data if p is not None else None, smp.ctypes.data)
+                     _addr(p) if p is not None else None, _addr(smp))
         del keep
         self._obs = None
         return p, smp
