@@ -133,8 +133,10 @@ int bs_last_stats(const bs_sim* sim, bs_stats* out);
  *      results) in one round trip: the state is reset to |0...0>, the ops are applied, and
  *      probs_out (2^n doubles, may be null) and samples_out (shots basis indices, bs_sample's
  *      generator with this seed) are filled.  The handle keeps the final state, as after
- *      bs_reinit + bs_evolve.  State vectors of at most 12 qubits (complex128 runs in one CTA; other
- *      cases take the usual kernels with the same results). */
+ *      bs_reinit + bs_evolve.  State vectors of at most 12 qubits (complex128 runs in one CTA that
+ *      reads the plan from and writes the results into host-mapped memory, and the host polls a
+ *      completion word instead of synchronising; other cases take the usual kernels with the same
+ *      results).  bs_last_stats then reports the kernel's own device time. */
 int bs_run_small(bs_sim* sim, const bs_op* ops, int64_t n_ops, int64_t shots, uint64_t seed, double* probs_out,
                  int64_t* samples_out);
 
