@@ -434,7 +434,7 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
     s->stats_pending = false;
     if (!s->defer_sync) s->tc_events_used = 0;   // deferred evolves keep their launch events for the caller
     s->alias_valid = false;
-    if (!s->capturing) cudaEventRecord(s->ev0, s->stream);
+    if (!s->capturing && !s->collect) cudaEventRecord(s->ev0, s->stream);   // a plan-only call times nothing
     std::vector<HostGate> pending, lowered;
     const int nb = bs_vec_bits(s);
     int phys[64];   // physical endian bit of each logical one
