@@ -442,6 +442,15 @@ def ghz_bench(bs, reps=2000, cpu=False):
         p, s = sim.run(ops, 1000, seed=r)
     dt = (time.perf_counter() - t0) / reps
     ok = abs(p[0] - 0.5) < 1e-15 and abs(p[-1] - 0.5) < 1e-15 and set(np.unique(s)) <= {0, 1023}
+    # a different circuit every call (GHZ-10 then Rz with a fresh angle on qubit 9): nothing of the
+    # previous call's plan can be reused
+    angles = np.random.default_rng(3).uniform(0, 2 * np.pi, reps // 4)
+    variants = [ops + [bs.Instruction(bs.Rz(float(a)), [9])] for a in angles]
+    t0 = time.perf_counter()
+    for r, v in enumerate(variants):
+        pv, sv = sim.run(v, 1000, seed=r)
+    dt_distinct = (time.perf_counter() - t0) / len(variants)
+    ok = ok and abs(pv[0] - 0.5) < 1e-13 and abs(pv[-1] - 0.5) < 1e-13   # float-float phases: ~2^-46
     for r in range(50):
         sim.reinit(10, 1000)
         sim.evolve(ops)
@@ -461,7 +470,11 @@ def ghz_bench(bs, reps=2000, cpu=False):
     sim.evolve(ops)
     ok = ok and np.array_equal(sim.probabilities(), p) and np.array_equal(sim.samples(reps), s)
     out = {"us_per_circuit": round(dt * 1e6, 1), "circuits_per_s": round(1 / dt, 1),
-           "api": "StateVectorSimulator.run (bs_run_small)", "four_calls_us_per_circuit": round(dt4 * 1e6, 1),
+           "api": "StateVectorSimulator.run (bs_run_small)",
+           "us_per_circuit_distinct": round(dt_distinct * 1e6, 1),
+           "note": "us_per_circuit: the same circuit every call (its plan is reused); distinct: a new "
+                   "Rz angle every call (planned every call)",
+           "four_calls_us_per_circuit": round(dt4 * 1e6, 1),
            "checked": bool(ok)}
     if cpu:
         out["cpu_baseline"] = ghz_cpu_port(reps)

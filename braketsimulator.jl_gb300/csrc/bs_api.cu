@@ -553,15 +553,54 @@ int bs_run_small(bs_sim* s, const bs_op* ops, int64_t n_ops, int64_t shots, uint
     if (s->capturing) return bs_fail(s, BS_ERR_STATE, "bs_run_small: not during graph capture");
     if (shots < 0 || (shots > 0 && !samples_out)) return bs_fail(s, BS_ERR_INVALID_ARG, "bad shot buffer");
     const int64_t dim = (int64_t)1 << s->n;
-    std::vector<Sweep> sweeps;
-    // plan the instruction list as bs_evolve does (lowering, SWAP relabelling, diagonal folding), launching nothing
-    s->collect = &sweeps;
-    const bool defer = s->defer_sync;
-    s->defer_sync = true;
-    int rc = bs_evolve(s, ops, n_ops, BS_NOISE_REFERENCE);
-    s->defer_sync = defer;
-    s->collect = nullptr;
-    if (rc) return rc;
+    // The list's exact bytes: the qubit count and tile setting, every op struct without its matrix
+    // pointer, every matrix's values.  The same bytes as the last call reuse its plan.  Lists with
+    // a malformed op or more than 1 MiB of matrices are planned every time (bs_evolve reports errors).
+    std::vector<char> key;
+    bool keyed = n_ops >= 0 && (n_ops == 0 || ops);
+    if (keyed) {
+        const int head[2] = {s->n, bs_tile_bits(s)};
+        key.insert(key.end(), (const char*)head, (const char*)head + sizeof(head));
+        size_t mat_bytes = 0;
+        for (int64_t i = 0; i < n_ops && keyed; i++) {
+            bs_op o = ops[i];
+            const double* m = o.matrix;
+            o.matrix = nullptr;
+            key.insert(key.end(), (const char*)&o, (const char*)&o + sizeof(o));
+            if (o.kind == 2) continue;
+            if (o.kind != 0 || !m || o.n_targets < 1 || o.n_targets > BS_MAX_TARGETS) { keyed = false; break; }
+            const size_t d = (size_t)1 << o.n_targets;
+            const size_t nd = 2 * ((o.flags & BS_GATE_DIAGONAL) ? d : d * d);
+            mat_bytes += nd * sizeof(double);
+            if (mat_bytes > ((size_t)1 << 20)) { keyed = false; break; }
+            key.insert(key.end(), (const char*)m, (const char*)(m + nd));
+        }
+    }
+    int rc = BS_OK;
+    bool in_tile = true;   // the plan has an in-tile kernel for every gate (else the usual path runs)
+    if (!(keyed && s->small_valid && key == s->small_key)) {
+        std::vector<Sweep> sweeps;
+        // plan the instruction list as bs_evolve does (lowering, SWAP relabelling, diagonal folding),
+        // launching nothing
+        s->small_valid = false;
+        s->collect = &sweeps;
+        const bool defer = s->defer_sync;
+        s->defer_sync = true;
+        rc = bs_evolve(s, ops, n_ops, BS_NOISE_REFERENCE);
+        s->defer_sync = defer;
+        s->collect = nullptr;
+        if (rc) return rc;
+        rc = bs_small_pack(s, sweeps, s->small_plan);
+        if (rc && rc != BS_ERR_UNSUPPORTED) return rc;
+        in_tile = rc == BS_OK;
+        if (in_tile && keyed) {
+            s->small_key.swap(key);
+            s->small_valid = true;
+        }
+    } else {
+        s->stats = bs_stats{};
+        s->stats_pending = false;
+    }
     // mapped layout: the completion word and the kernel's start and end times (256 bytes), the
     // probabilities, the shots, then room for the plan
     const size_t pb = ((size_t)dim * 8 + 255) & ~(size_t)255, sb = ((size_t)shots * 8 + 255) & ~(size_t)255;
@@ -587,7 +626,8 @@ int bs_run_small(bs_sim* s, const bs_op* ops, int64_t n_ops, int64_t shots, uint
         dsamp = (int64_t*)((char*)s->scratch + pb);
         cudaEventRecord(s->ev0, s->stream);
     }
-    rc = bs_run_small_sweeps(s, sweeps, dprobs, shots, seed, dsamp, ddone, ticket, mapped ? &io : nullptr);
+    rc = in_tile ? bs_small_launch(s, s->small_plan, dprobs, shots, seed, dsamp, ddone, ticket, mapped ? &io : nullptr)
+                 : BS_ERR_UNSUPPORTED;
     if (rc == BS_ERR_UNSUPPORTED) {
         // a gate without an in-tile kernel (dense on more than 4 qubits) or a complex64 state: the usual
         // path, with the same results

@@ -82,6 +82,15 @@ struct BsTuning {
     int adj_segments = -1;   // adjoint gradients: forward segments (checkpoints + 1); -1 = from memory
 };
 
+// The packed plan of one small-circuit run (bs_run_small): the whole state is one tile, so the plan is
+// the gate table, its matrices and permutations, and the largest dense or monomial target count.
+struct SmallPlan {
+    std::vector<TileGate> tg;
+    std::vector<float4> mats;
+    std::vector<int32_t> perms;
+    int kmax = 1;
+};
+
 struct bs_sim {
     int kind = BS_KIND_SV;
     int n = 0;                    // qubits
@@ -123,6 +132,12 @@ struct bs_sim {
     std::vector<std::pair<char*, size_t>> arena;   // chunks (pointer, capacity)
     size_t arena_used = 0;                          // bytes used in the last chunk
     std::vector<Sweep>* collect = nullptr;          // bs_evolve plans into this list instead of launching
+    // bs_run_small: the plan of the last instruction list, kept with the list's exact bytes (op structs
+    // without their matrix pointers, the matrix values, the qubit count and tile setting) so that the
+    // same list again skips the planning
+    std::vector<char> small_key;
+    SmallPlan small_plan;
+    bool small_valid = false;
 };
 
 // ---- helpers implemented in bs_api.cu
@@ -197,5 +212,8 @@ struct SmallIO {
     size_t plan_cap;
     int64_t* dtimes;
 };
-int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dprobs, int64_t shots, uint64_t seed,
-                        int64_t* dsamples, int64_t* done, int64_t ticket, const SmallIO* io);
+// Pack the planned sweeps of a small run; BS_ERR_UNSUPPORTED (nothing packed) when a gate has no in-tile
+// kernel or the state is not a complex128 state vector of at most 12 qubits.
+int bs_small_pack(const bs_sim* s, const std::vector<Sweep>& sweeps, SmallPlan& out);
+int bs_small_launch(bs_sim* s, const SmallPlan& plan, double* dprobs, int64_t shots, uint64_t seed,
+                    int64_t* dsamples, int64_t* done, int64_t ticket, const SmallIO* io);

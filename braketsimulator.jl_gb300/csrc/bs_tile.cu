@@ -1894,13 +1894,15 @@ __global__ void __launch_bounds__(512) k_small_run(double2* __restrict__ psi, in
 
 }  // namespace
 
-int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dprobs, int64_t shots, uint64_t seed,
-                        int64_t* dsamples, int64_t* done, int64_t ticket, const SmallIO* io) {
+int bs_small_pack(const bs_sim* s, const std::vector<Sweep>& sweeps, SmallPlan& out) {
     const int n = s->n;
     if (s->kind != BS_KIND_SV || s->precision != BS_PREC_C128 || n > 12) return BS_ERR_UNSUPPORTED;
-    std::vector<TileGate> tg;
-    std::vector<float4> mats;
-    std::vector<int32_t> perms;
+    std::vector<TileGate>& tg = out.tg;
+    std::vector<float4>& mats = out.mats;
+    std::vector<int32_t>& perms = out.perms;
+    tg.clear();
+    mats.clear();
+    perms.clear();
     int kmax = 1;
     std::vector<HostGate> merged;
     for (const Sweep& sw : sweeps) {
@@ -1931,6 +1933,17 @@ int bs_run_small_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps, double* dpr
             tg.push_back(t);
         }
     }
+    out.kmax = kmax;
+    return BS_OK;
+}
+
+int bs_small_launch(bs_sim* s, const SmallPlan& plan, double* dprobs, int64_t shots, uint64_t seed,
+                    int64_t* dsamples, int64_t* done, int64_t ticket, const SmallIO* io) {
+    const int n = s->n;
+    const std::vector<TileGate>& tg = plan.tg;
+    const std::vector<float4>& mats = plan.mats;
+    const std::vector<int32_t>& perms = plan.perms;
+    const int kmax = plan.kmax;
     auto al = [](int64_t x) { return (x + 255) & ~(int64_t)255; };
     const int64_t b_tg = al((int64_t)(tg.size() + 1) * (int64_t)sizeof(TileGate));
     const int64_t b_m = al((int64_t)(mats.size() + 1) * (int64_t)sizeof(float4));

@@ -80,6 +80,27 @@ def test_run_permutation_heavy_circuits(n):
     assert np.all(np.abs(ref[s]) ** 2 > 1e-14)
 
 
+def test_run_reuses_the_plan_only_for_the_same_list():
+    """The plan of the last list is reused when the next list has the same op structs and matrix
+    values; a changed angle, target or length is planned afresh.  Every result against the oracle."""
+    sim = bs.StateVectorSimulator(8, 300)
+    base = ghz(8)
+    lists = [base + [bs.Instruction(bs.Ry(0.3), [2])], base + [bs.Instruction(bs.Ry(0.3), [2])],
+             base + [bs.Instruction(bs.Ry(0.7), [2])], base + [bs.Instruction(bs.Ry(0.7), [5])],
+             base, base + [bs.Instruction(bs.Ry(0.3), [2])]]
+    first = None
+    for i, ops in enumerate(lists):
+        p, s = sim.run(ops, 300, seed=5)
+        ref = oracle.OracleSV(8).evolve(ops).psi
+        assert rel_err(sim.state_vector, ref) < 1e-12
+        assert np.max(np.abs(p - np.abs(ref) ** 2)) < 1e-14
+        assert np.array_equal(sim.samples(5), s)
+        if i == 0:
+            first = (p, s)
+        if i in (1, 5):
+            assert np.array_equal(p, first[0]) and np.array_equal(s, first[1])
+
+
 def test_run_repeats_and_resets():
     """Each call starts from |0...0> whatever the handle held; the same seed gives the same shots."""
     ops = ghz(6) + [bs.Instruction(bs.Ry(0.4), [3])]
