@@ -99,6 +99,8 @@ def test_run_reuses_the_plan_only_for_the_same_list():
             first = (p, s)
         if i in (1, 5):
             assert np.array_equal(p, first[0]) and np.array_equal(s, first[1])
+        st = sim.last_stats()
+        assert st["kernel_launches"] == 1 and st["gates"] >= 1 and st["gpu_ms"] > 0
 
 
 def test_run_repeats_and_resets():
@@ -126,6 +128,8 @@ def test_run_falls_back_for_wide_gates_and_complex64():
     assert np.max(np.abs(p - np.abs(ref) ** 2)) < 1e-13
     usual = bs.StateVectorSimulator(7, 300).evolve(ops)
     assert np.array_equal(usual.samples(2), s)
+    p2, s2 = sim.run(ops, 300, seed=2)          # the same list again: the usual path again
+    assert np.array_equal(p2, p) and np.array_equal(s2, s)
     s64 = bs.StateVectorSimulator(7, 300, precision="c64")
     p64, q64 = s64.run(ops, 300, seed=2)
     assert np.max(np.abs(p64 - np.abs(ref) ** 2)) < 1e-6
