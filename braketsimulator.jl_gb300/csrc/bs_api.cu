@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <iterator>
 #include <cstring>
 #include <new>
 #include "bs_internal.h"
@@ -489,7 +490,7 @@ int bs_evolve(bs_sim* s, const bs_op* ops, int64_t n_ops, unsigned noise_mode) {
         bs_plan_sweeps(pending, bs_vec_bits(s), bs_tile_bits(s), sw);
         pending.clear();
         if (s->collect) {   // bs_run_small: plan only
-            s->collect->insert(s->collect->end(), sw.begin(), sw.end());
+            s->collect->insert(s->collect->end(), std::make_move_iterator(sw.begin()), std::make_move_iterator(sw.end()));
             return BS_OK;
         }
         return bs_run_sweeps(s, sw);

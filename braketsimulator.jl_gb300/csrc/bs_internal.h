@@ -163,7 +163,8 @@ int bs_lower_gate(bs_sim* s, const double* matrix, int k, const int* targets, in
                   std::vector<HostGate>& out);
 int bs_lower_kraus_physical(bs_sim* s, const double* kraus, int nk, int k, const int* targets,
                             unsigned flags, std::vector<HostGate>& out);
-void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, int tile_bits, std::vector<Sweep>& out);
+// The gates are moved into the sweeps (the input is left with moved-from gates).
+void bs_plan_sweeps(std::vector<HostGate>& gates, int n_bits, int tile_bits, std::vector<Sweep>& out);
 // Tuned values of a handle (its setting, else the environment, else the default)
 int bs_tile_bits(const bs_sim* s);
 int bs_tile_threads(const bs_sim* s);

@@ -105,8 +105,8 @@ int bs_lower_gate(bs_sim* s, const double* matrix, int k, const int* targets, in
     for (double v : g.mat)
         if (!std::isfinite(v)) return bs_fail(s, BS_ERR_INVALID_ARG, "matrix has non-finite entries");
     classify(g);
-    auto put = [&](int offset, bool conj) {
-        HostGate h = g;
+    auto put = [&](int offset, bool conj, bool last) {
+        HostGate h = last ? std::move(g) : g;
         for (int j = 0; j < k; j++) h.ebit[j] = offset + (nq - 1 - ct[j]);
         h.cmask = 0;
         h.cval = 0;
@@ -125,10 +125,10 @@ int bs_lower_gate(bs_sim* s, const double* matrix, int k, const int* targets, in
         out.push_back(std::move(h));
     };
     if (dm_superop) {
-        put(s->n, false);   // column bits: U
-        put(0, true);       // row bits: conj(U)
+        put(s->n, false, false);   // column bits: U
+        put(0, true, true);        // row bits: conj(U)
     } else {
-        put(0, false);
+        put(0, false, true);
     }
     return BS_OK;
 }
@@ -213,7 +213,7 @@ double bs_tc_cost(const bs_sim* s) {
 // Greedy sweep planner.  A gate may move ahead of gates it does not share a bit
 // with; a dense or monomial gate needs its target bits inside the tile, a
 // diagonal gate or a control never does (their bits are read from the index).
-void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, int tile_bits, std::vector<Sweep>& out) {
+void bs_plan_sweeps(std::vector<HostGate>& gates, int n_bits, int tile_bits, std::vector<Sweep>& out) {
     const int T = std::min(tile_bits, n_bits);
     const int L = std::min(BS_TILE_LOW_BITS, T);
     const int cap = T - L;
@@ -250,14 +250,14 @@ void bs_plan_sweeps(const std::vector<HostGate>& gates, int n_bits, int tile_bit
             bool too_big = (g.kind != 1) && (g.k > BS_TILE_MAXK || __builtin_popcountll(need(g)) > cap);
             if (too_big) {
                 // a gate no tile can hold runs in a sweep of its own
-                if (sw.gates.empty()) { sw.gates.push_back(g); done[i] = 1; remaining--; big_alone = true; }
+                if (sw.gates.empty()) { sw.gates.push_back(std::move(gates[i])); done[i] = 1; remaining--; big_alone = true; }
                 blocked |= t;
                 break;
             }
             if (nchosen + add <= cap) {
                 chosen |= nb;
                 nchosen += add;
-                sw.gates.push_back(g);
+                sw.gates.push_back(std::move(gates[i]));
                 done[i] = 1;
                 remaining--;
             } else {
