@@ -102,21 +102,40 @@ _LOWER_CACHE_MAX = 1 << 16
 
 _BSOP_SIZE = C.sizeof(_abi.BsOp)
 _OFF_NT, _OFF_T0, _OFF_MAT = _abi.BsOp.n_targets.offset, _abi.BsOp.targets.offset, _abi.BsOp.matrix.offset
+_ONE_TARGET_OP = bytearray(_BSOP_SIZE)   # a gate op with one target, the rest zero
+struct.pack_into("<i", _ONE_TARGET_OP, _OFF_NT, 1)
+_ONE_TARGET_OP = bytes(_ONE_TARGET_OP)
 _ROTATIONS = (Rx, Ry, Rz)
 # gate types whose lowering is cached by value (type, angles, pow_exponent, targets): every Gate
 # type but the matrix-carrying ones (Unitary, Control), added as they are first lowered
 _BY_VALUE = set()
 
 
+def _rotation_buffer(op) -> np.ndarray:
+    """matrix_rep of Rx/Ry/Rz as the engine's interleaved buffer; at pow_exponent 1 the entries are
+    written directly (the same doubles, signed zeros included, as the complex arithmetic of raw_at)."""
+    if op.pow_exponent != 1:
+        return _abi.cplx_buffer(op.matrix_rep())
+    t = op.angle[0]
+    s, c = math.sin(t / 2.0), math.cos(t / 2.0)
+    tp = type(op)
+    if tp is Rx:      # [[c, -i s], [-i s, c]]
+        v = (c, 0.0, 0.0, -s, 0.0, -s, c, 0.0)
+    elif tp is Ry:    # [[c, -s], [s, c]]
+        v = (c, 0.0, -s, 0.0, s, 0.0, c, 0.0)
+    else:             # [[c - i s, 0], [0, c + i s]]
+        v = (c, 0.0 - s, 0.0, 0.0, 0.0, 0.0, c, 0.0 + s)
+    return np.array(v, dtype=np.float64)
+
+
 def _rotation_op(op, q: int):
     """The lowering of a 1-qubit rotation (what lower_gate gives: its dense matrix_rep, no flags),
     without the generic dispatch: rotations in variational and random circuits rarely repeat an
     angle, so they miss the cache and their lowering cost is the batch's host time."""
-    buf = _abi.cplx_buffer(op.matrix_rep())
-    b = bytearray(_BSOP_SIZE)
-    struct.pack_into("<i", b, _OFF_NT, 1)
+    buf = _rotation_buffer(op)
+    b = bytearray(_ONE_TARGET_OP)
     struct.pack_into("<i", b, _OFF_T0, q)
-    struct.pack_into("<Q", b, _OFF_MAT, buf.ctypes.data)
+    struct.pack_into("<Q", b, _OFF_MAT, _addr(buf))
     return [(bytes(b), buf)]
 
 

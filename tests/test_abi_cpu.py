@@ -149,3 +149,9 @@ def test_rotation_fast_lowering_matches_generic_lowering():
             assert (o.kind, o.flags, o.n_targets, o.targets[0], o.n_controls, o.n_matrices) == (0, lg.flags, 1, q, 0, 0)
             assert np.array_equal(buf, bs._abi.cplx_buffer(lg.matrix))
             assert S._gate_ops(g, (q,))[0][1].dtype == np.float64
+    # at pow_exponent 1 the entries are written directly: the same bytes as the complex arithmetic,
+    # signed zeros included
+    for cls in (G.Rx, G.Ry, G.Rz):
+        for a in [0.0, -0.0, np.pi, -np.pi, 2 * np.pi, 1e-300, -1e-300] + list(rng.uniform(-50, 50, 400)):
+            g = cls(float(a))
+            assert S._rotation_buffer(g).tobytes() == bs._abi.cplx_buffer(g.matrix_rep()).tobytes()
