@@ -50,10 +50,19 @@ def _ops_for(instructions, dm: bool, noise_mode: int):
     keep = []
     skip = (Measure, Reset, Barrier, Delay)
     cache = _LOWER_CACHE
+    rot_at, rot_vals = [], []   # 1-qubit rotations: their ops, and their matrices for one shared buffer
     for ix in instructions:
         op = ix.operator
         t = ix.target
         tp = type(op)
+        if tp in _ROT_TYPES and len(t) == 1 and op.pow_exponent == 1:
+            rot_at.append(len(ops))
+            o = _ONE_TARGET_OPS.get(t[0])
+            if o is None:
+                o = _ONE_TARGET_OPS[t[0]] = _one_target_op(t[0])
+            ops.append(o)
+            rot_vals.extend(_rotation_values(op))
+            continue
         if tp in _BY_VALUE:
             # a fixed gate lowered before (the common case of repeated circuits): no dispatch
             hit = cache.get((tp, op.angle, op.pow_exponent, t))
@@ -90,6 +99,12 @@ def _ops_for(instructions, dm: bool, noise_mode: int):
     if n == 0:
         return (_abi.BsOp * 1)(), 0, keep
     arr = (_abi.BsOp * n).from_buffer_copy(b"".join(ops))
+    if rot_at:
+        # every rotation's matrix in one buffer, 8 doubles each; their ops point into it
+        vals = np.array(rot_vals, dtype=np.float64)
+        keep.append(vals)
+        words = np.frombuffer(arr, dtype=np.uint64).reshape(n, _BSOP_SIZE // 8)
+        words[rot_at, _OFF_MAT // 8] = np.uint64(_addr(vals)) + np.uint64(64) * np.arange(len(rot_at), dtype=np.uint64)
     return arr, n, keep
 
 
@@ -106,26 +121,38 @@ _ONE_TARGET_OP = bytearray(_BSOP_SIZE)   # a gate op with one target, the rest z
 struct.pack_into("<i", _ONE_TARGET_OP, _OFF_NT, 1)
 _ONE_TARGET_OP = bytes(_ONE_TARGET_OP)
 _ROTATIONS = (Rx, Ry, Rz)
+_ROT_TYPES = frozenset(_ROTATIONS)
+_ONE_TARGET_OPS: dict = {}   # target -> _one_target_op(target)
 # gate types whose lowering is cached by value (type, angles, pow_exponent, targets): every Gate
 # type but the matrix-carrying ones (Unitary, Control), added as they are first lowered
 _BY_VALUE = set()
 
 
-def _rotation_buffer(op) -> np.ndarray:
-    """matrix_rep of Rx/Ry/Rz as the engine's interleaved buffer; at pow_exponent 1 the entries are
-    written directly (the same doubles, signed zeros included, as the complex arithmetic of raw_at)."""
-    if op.pow_exponent != 1:
-        return _abi.cplx_buffer(op.matrix_rep())
+def _rotation_values(op) -> tuple:
+    """The 8 doubles (row-major, interleaved) of Rx/Ry/Rz at pow_exponent 1, written directly: the
+    same doubles, signed zeros included, as the complex arithmetic of raw_at."""
     t = op.angle[0]
     s, c = math.sin(t / 2.0), math.cos(t / 2.0)
     tp = type(op)
     if tp is Rx:      # [[c, -i s], [-i s, c]]
-        v = (c, 0.0, 0.0, -s, 0.0, -s, c, 0.0)
-    elif tp is Ry:    # [[c, -s], [s, c]]
-        v = (c, 0.0, -s, 0.0, s, 0.0, c, 0.0)
-    else:             # [[c - i s, 0], [0, c + i s]]
-        v = (c, 0.0 - s, 0.0, 0.0, 0.0, 0.0, c, 0.0 + s)
-    return np.array(v, dtype=np.float64)
+        return (c, 0.0, 0.0, -s, 0.0, -s, c, 0.0)
+    if tp is Ry:      # [[c, -s], [s, c]]
+        return (c, 0.0, -s, 0.0, s, 0.0, c, 0.0)
+    return (c, 0.0 - s, 0.0, 0.0, 0.0, 0.0, c, 0.0 + s)   # Rz: [[c - i s, 0], [0, c + i s]]
+
+
+def _rotation_buffer(op) -> np.ndarray:
+    """matrix_rep of Rx/Ry/Rz as the engine's interleaved buffer."""
+    if op.pow_exponent != 1:
+        return _abi.cplx_buffer(op.matrix_rep())
+    return np.array(_rotation_values(op), dtype=np.float64)
+
+
+def _one_target_op(q: int) -> bytes:
+    """A gate op on one target q with no matrix yet (the rest zero)."""
+    b = bytearray(_ONE_TARGET_OP)
+    struct.pack_into("<i", b, _OFF_T0, q)
+    return bytes(b)
 
 
 def _rotation_op(op, q: int):

@@ -155,3 +155,32 @@ def test_rotation_fast_lowering_matches_generic_lowering():
         for a in [0.0, -0.0, np.pi, -np.pi, 2 * np.pi, 1e-300, -1e-300] + list(rng.uniform(-50, 50, 400)):
             g = cls(float(a))
             assert S._rotation_buffer(g).tobytes() == bs._abi.cplx_buffer(g.matrix_rep()).tobytes()
+
+
+def test_lowered_op_arrays_match_gate_by_gate_lowering():
+    """_ops_for puts every pow-1 rotation's matrix into one buffer shared by the list: each op must
+    equal the gate-by-gate lowering's (struct fields, and the matrix bytes it points at)."""
+    import ctypes as C
+    import numpy as np
+    from braketsimulator_gb300 import gates as G, simulators as S
+    rng = np.random.default_rng(5)
+    kinds = [lambda q: (G.Rx(float(rng.uniform(-9, 9))), (q,)), lambda q: (G.Ry(float(rng.uniform(-9, 9))), (q,)),
+             lambda q: (G.Rz(float(rng.uniform(-9, 9))), (q,)), lambda q: (G.Rz(0.0), (q,)),
+             lambda q: (G.Rx(0.4, pow_exponent=2.0), (q,)), lambda q: (G.H(), (q,)),
+             lambda q: (G.CNot(), (q, (q + 1) % 6)), lambda q: (G.XX(0.3), (q, (q + 2) % 6)),
+             lambda q: (G.Unitary(np.eye(2) * np.exp(0.1j)), (q,))]
+    for trial in range(20):
+        ops = []
+        for _ in range(40):
+            g, t = kinds[int(rng.integers(len(kinds)))](int(rng.integers(6)))
+            ops.append(bs.Instruction(g, list(t)))
+        arr, n, keep = S._ops_for(ops, False, 0)
+        expect = [pair for ix in ops for pair in S._gate_ops(ix.operator, tuple(ix.target))]
+        assert n == len(expect)
+        size = C.sizeof(bs._abi.BsOp)
+        off = bs._abi.BsOp.matrix.offset
+        for i, (raw, buf) in enumerate(expect):
+            got = bytes(C.string_at(C.addressof(arr) + i * size, size))
+            assert got[:off] == raw[:off] and got[off + 8:] == raw[off + 8:]
+            nbytes = buf.size * 8
+            assert C.string_at(arr[i].matrix, nbytes) == buf.tobytes()
