@@ -199,14 +199,13 @@ int64_t bs_alias_parallel_scratch(int64_t n);
 int bs_alias_parallel(bs_sim* s, const double* dprobs, int64_t n, double wsum, double* ap, int64_t* alias, void* work);
 
 // ---- small state vectors in one CTA (bs_tile.cu, bs_sample.cu)
-// |0...0>, the planned sweeps' gates, the state written back, its probabilities into dprobs and `shots`
-// draws of bs_sample's generator with `seed` into dsamples, in one launch (dprobs and dsamples: device
-// addresses, mapped host memory included); at its end the kernel writes `ticket` into *done (a
-// host-mapped word, may be null) once every result is visible to the host.  BS_ERR_UNSUPPORTED
-// (nothing launched) when a gate has no in-tile kernel or the state is not a complex128 state vector
-// of at most 12 qubits.  io (may be null): host-mapped memory for the plan (written at hplan, read by
-// the kernel at dplan, when it fits in plan_cap bytes; otherwise the plan is uploaded) and for the
-// kernel's start and end times (globaltimer nanoseconds, at dtimes[0] and dtimes[1]).
+// bs_small_launch: |0...0>, the packed plan's gates, the state written back, its probabilities into
+// dprobs and `shots` draws of bs_sample's generator with `seed` into dsamples, in one launch (dprobs
+// and dsamples: device addresses, mapped host memory included); at its end the kernel writes `ticket`
+// into *done (a host-mapped word, may be null) once every result is visible to the host.  io (may be
+// null): host-mapped memory for the plan (written at hplan, read by the kernel at dplan, when it fits
+// in plan_cap bytes; otherwise the plan is uploaded) and for the kernel's start and end times
+// (globaltimer nanoseconds, at dtimes[0] and dtimes[1]).
 struct SmallIO {
     char* hplan;
     char* dplan;
