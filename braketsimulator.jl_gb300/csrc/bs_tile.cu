@@ -910,216 +910,6 @@ __global__ void __launch_bounds__(kThreads) k_dense_big_c64(float2* __restrict__
     }
 }
 
-// ---------------------------------------------------------------------------
-// Register-blocked variant for full 2^12 tiles whose non-diagonal gates are 1-target:
-// each of the 256 threads keeps 16 amplitudes in registers, indexed by 4 "register
-// bits" of the tile.  A segment is a run of gates whose dense/monomial targets are
-// register bits: they run without shared memory or barriers.  Between segments the
-// tile goes through shared memory once to change which bits are register bits.
-struct RBSeg {
-    int32_t reg[4];   // tile positions held in registers (bit k of the register index)
-    int32_t g0, g1;   // gate range in the sweep's gate table
-};
-
-template <int S>
-__device__ __forceinline__ void rb_dense1(cff (&a)[16], int jt, const int (&rbm)[4], uint32_t lcm, uint32_t lcv,
-                                          const cff& m00, const cff& m01, const cff& m10, const cff& m11) {
-#pragma unroll
-    for (int r = 0; r < 16; r++) {
-        if ((r >> S) & 1) continue;
-        const int r1 = r | (1 << S);
-        const int j = jt | ((r & 1) ? rbm[0] : 0) | ((r & 2) ? rbm[1] : 0) | ((r & 4) ? rbm[2] : 0) | ((r & 8) ? rbm[3] : 0);
-        if ((j & (int)lcm) != (int)lcv) continue;
-        ffacc ar, ai;
-        cmac_first(ar, ai, m00, a[r]);
-        cmac(ar, ai, m01, a[r1]);
-        const cff y0 = cdone(ar, ai);
-        cmac_first(ar, ai, m10, a[r]);
-        cmac(ar, ai, m11, a[r1]);
-        a[r1] = cdone(ar, ai);
-        a[r] = y0;
-    }
-}
-
-template <int S>
-__device__ __forceinline__ void rb_mono1(cff (&a)[16], int jt, const int (&rbm)[4], uint32_t lcm, uint32_t lcv,
-                                         int r0, int p0, int r1t, int p1) {
-    // column 0 -> row r0 with phase i^p0, column 1 -> row r1t with phase i^p1
-#pragma unroll
-    for (int r = 0; r < 16; r++) {
-        if ((r >> S) & 1) continue;
-        const int r1 = r | (1 << S);
-        const int j = jt | ((r & 1) ? rbm[0] : 0) | ((r & 2) ? rbm[1] : 0) | ((r & 4) ? rbm[2] : 0) | ((r & 8) ? rbm[3] : 0);
-        if ((j & (int)lcm) != (int)lcv) continue;
-        const cff x0 = cmul_ipow(a[r], p0), x1 = cmul_ipow(a[r1], p1);
-        if (r0 == 0) { a[r] = x0; a[r1] = x1; } else { a[r1] = x0; a[r] = x1; }
-        (void)r1t;
-    }
-}
-
-__device__ __forceinline__ void rb_diag(cff (&a)[16], int jt, const int (&rbm)[4], const TileGate& g,
-                                        const float4* __restrict__ m, int64_t base) {
-    const int k = g.k;
-    int cst = 0;                     // bits of the diagonal index fixed by the tile's base
-    int tp[BS_TILE_MAXK];
-    for (int q = 0; q < k; q++) {
-        tp[q] = g.tbit[q];
-        if (tp[q] < 0) cst |= (int)((base >> g.gbit[q]) & 1) << q;
-    }
-    const uint32_t lcm = g.lc_mask, lcv = g.lc_val;
-#pragma unroll
-    for (int r = 0; r < 16; r++) {
-        const int j = jt | ((r & 1) ? rbm[0] : 0) | ((r & 2) ? rbm[1] : 0) | ((r & 4) ? rbm[2] : 0) | ((r & 8) ? rbm[3] : 0);
-        if ((j & (int)lcm) != (int)lcv) continue;
-        int di = cst;
-        for (int q = 0; q < k; q++) if (tp[q] >= 0) di |= ((j >> tp[q]) & 1) << q;
-        const float4 d = __ldg(m + di);
-        if (d.y == 0.f && d.w == 0.f) {
-            if (d.z == 0.f && d.x == 1.f) continue;
-            if (d.z == 0.f && d.x == -1.f) { a[r] = cmul_ipow(a[r], 2); continue; }
-            if (d.x == 0.f && d.z == 1.f) { a[r] = cmul_ipow(a[r], 1); continue; }
-            if (d.x == 0.f && d.z == -1.f) { a[r] = cmul_ipow(a[r], 3); continue; }
-        }
-        a[r] = cmul(f4m(d), a[r]);
-    }
-}
-
-__device__ __forceinline__ void rb_to_smem(float4* sm, const cff (&a)[16], int jt, const int (&rbm)[4]) {
-#pragma unroll
-    for (int r = 0; r < 16; r++) {
-        const int j = jt | ((r & 1) ? rbm[0] : 0) | ((r & 2) ? rbm[1] : 0) | ((r & 4) ? rbm[2] : 0) | ((r & 8) ? rbm[3] : 0);
-        sm[j] = c4f(a[r]);
-    }
-}
-__device__ __forceinline__ void rb_from_smem(const float4* sm, cff (&a)[16], int jt, const int (&rbm)[4]) {
-#pragma unroll
-    for (int r = 0; r < 16; r++) {
-        const int j = jt | ((r & 1) ? rbm[0] : 0) | ((r & 2) ? rbm[1] : 0) | ((r & 4) ? rbm[2] : 0) | ((r & 8) ? rbm[3] : 0);
-        a[r] = f4c(sm[j]);
-    }
-}
-
-// MINB = resident CTAs per SM the register budget is sized for (1: no spills, 2: twice the warps)
-template <int MINB>
-__global__ void __launch_bounds__(kThreads, MINB) k_tile_rb(double2* __restrict__ psi, SweepDesc d,
-                                                      const RBSeg* __restrict__ segs, int nseg, int64_t tile0) {
-    extern __shared__ float4 smem[];
-    constexpr int T = 12;
-    const int L = d.L, H = T - L;
-    int64_t* off_tab = reinterpret_cast<int64_t*>(smem + (1 << T));
-    __shared__ int64_t s_base;
-    const int64_t tile = tile0 + (int64_t)blockIdx.x;
-    if (threadIdx.x == 0) {
-        int64_t base = 0;
-        int src = 0;
-        for (int bit = 0; bit < d.n_bits; bit++)
-            if (!((d.tile_mask >> bit) & 1ULL)) { base |= ((tile >> src) & 1LL) << bit; src++; }
-        s_base = base;
-    }
-    for (int i = threadIdx.x; i < (1 << H); i += blockDim.x) {
-        int64_t o = 0;
-        for (int j = 0; j < H; j++) if ((i >> j) & 1) o |= 1LL << d.hi_bits[j];
-        off_tab[i] = o;
-    }
-    __syncthreads();
-    const int64_t base = s_base;
-    const int lowmask = (1 << L) - 1;
-    for (int j = threadIdx.x; j < (1 << T); j += blockDim.x) {
-        const int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
-        smem[j] = c4f(load_c128(__ldcs(psi + gidx)));
-    }
-    __syncthreads();
-    cff a[16];
-    for (int s = 0; s < nseg; s++) {
-        const RBSeg& sg = segs[s];
-        int rbm[4];
-        int tmask = (1 << T) - 1;
-#pragma unroll
-        for (int k = 0; k < 4; k++) { rbm[k] = 1 << sg.reg[k]; tmask &= ~rbm[k]; }
-        // deposit the thread index into the 8 non-register tile bits
-        int jt = 0, src = 0;
-        for (int b = 0; b < T; b++)
-            if ((tmask >> b) & 1) { jt |= (((int)threadIdx.x >> src) & 1) << b; src++; }
-        rb_from_smem(smem, a, jt, rbm);
-        for (int gi = sg.g0; gi < sg.g1; gi++) {
-            const TileGate& g = d.gates[gi];
-            if ((base & (int64_t)g.gc_mask) != (int64_t)g.gc_val) continue;
-            if (g.kind == 1) {
-                rb_diag(a, jt, rbm, g, d.mats + g.mat_off, base);
-                continue;
-            }
-            const int tpos = g.tbit[0];
-            const int slot = (tpos == sg.reg[0]) ? 0 : (tpos == sg.reg[1]) ? 1 : (tpos == sg.reg[2]) ? 2 : 3;
-            if (g.kind == 0) {
-                const float4* m = d.mats + g.mat_off;
-                const cff m00 = f4m(__ldg(m)), m01 = f4m(__ldg(m + 1)), m10 = f4m(__ldg(m + 2)), m11 = f4m(__ldg(m + 3));
-                switch (slot) {
-                    case 0: rb_dense1<0>(a, jt, rbm, g.lc_mask, g.lc_val, m00, m01, m10, m11); break;
-                    case 1: rb_dense1<1>(a, jt, rbm, g.lc_mask, g.lc_val, m00, m01, m10, m11); break;
-                    case 2: rb_dense1<2>(a, jt, rbm, g.lc_mask, g.lc_val, m00, m01, m10, m11); break;
-                    default: rb_dense1<3>(a, jt, rbm, g.lc_mask, g.lc_val, m00, m01, m10, m11); break;
-                }
-            } else {
-                const int32_t* p = d.perms + g.perm_off;
-                const int r0 = __ldg(p), p0 = __ldg(p + 1), r1t = __ldg(p + 2), p1 = __ldg(p + 3);
-                switch (slot) {
-                    case 0: rb_mono1<0>(a, jt, rbm, g.lc_mask, g.lc_val, r0, p0, r1t, p1); break;
-                    case 1: rb_mono1<1>(a, jt, rbm, g.lc_mask, g.lc_val, r0, p0, r1t, p1); break;
-                    case 2: rb_mono1<2>(a, jt, rbm, g.lc_mask, g.lc_val, r0, p0, r1t, p1); break;
-                    default: rb_mono1<3>(a, jt, rbm, g.lc_mask, g.lc_val, r0, p0, r1t, p1); break;
-                }
-            }
-        }
-        rb_to_smem(smem, a, jt, rbm);
-        __syncthreads();
-    }
-    for (int j = threadIdx.x; j < (1 << T); j += blockDim.x) {
-        const int64_t gidx = base | off_tab[j >> L] | (int64_t)(j & lowmask);
-        __stcs(psi + gidx, store_c128(f4c(smem[j])));
-    }
-}
-
-// Segments for a register-blocked sweep; empty when the sweep does not qualify.
-std::vector<RBSeg> rb_segments(const std::vector<TileGate>& tg, int64_t g0, int ng, int T) {
-    std::vector<RBSeg> segs;
-    if (T != 12) return segs;
-    for (int i = 0; i < ng; i++) {
-        const TileGate& g = tg[(size_t)(g0 + i)];
-        if (g.kind == 3) return {};
-        if (g.kind == 1) { if (g.k > BS_TILE_MAXK) return {}; continue; }
-        if (g.k != 1 || g.tbit[0] < 0) return {};
-    }
-    auto need = [&](int i) { const TileGate& g = tg[(size_t)(g0 + i)]; return g.kind == 1 ? -1 : g.tbit[0]; };
-    int i = 0;
-    while (i < ng) {
-        RBSeg s{};
-        int nr = 0;
-        // register bits: the next distinct 1-target positions in gate order
-        for (int j = i; j < ng && nr < 4; j++) {
-            int p = need(j);
-            if (p < 0) continue;
-            bool have = false;
-            for (int k = 0; k < nr; k++) have |= (s.reg[k] == p);
-            if (!have) s.reg[nr++] = p;
-        }
-        for (int p = 0; p < T && nr < 4; p++) {
-            bool have = false;
-            for (int k = 0; k < nr; k++) have |= (s.reg[k] == p);
-            if (!have) s.reg[nr++] = p;
-        }
-        s.g0 = (int32_t)i;          // relative to the sweep's first gate
-        int j = i;
-        for (; j < ng; j++) {
-            int p = need(j);
-            if (p < 0) continue;
-            if (p != s.reg[0] && p != s.reg[1] && p != s.reg[2] && p != s.reg[3]) break;
-        }
-        s.g1 = (int32_t)j;
-        segs.push_back(s);
-        i = j;
-    }
-    return segs;
-}
 
 inline float4 to_cff(double re, double im) {
     float4 v;
@@ -1496,32 +1286,15 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         }
         launches.push_back(std::move(ln));
     }
-    // register-blocked segments for the sweeps that qualify
-    // BS_TILE_VARIANT selects between equivalent kernels: "smem" (gate-by-gate in shared
-    // memory), "rb1" / "rb2" (register-blocked sized for 1 or 2 CTAs per SM)
-    static const std::string variant = [] { const char* v = getenv("BS_TILE_VARIANT"); return std::string(v ? v : "smem"); }();
-    const bool rb_off = variant == "smem";
-    const bool rb_one = variant == "rb1";
-    std::vector<RBSeg> segs;
-    std::vector<int64_t> seg0(launches.size(), -1), nseg(launches.size(), 0);
-    for (size_t li = 0; li < launches.size() && !rb_off; li++) {
-        if (launches[li].big || launches[li].tc_last >= 0) continue;
-        std::vector<RBSeg> ss = rb_segments(tg, launches[li].gate0, launches[li].n_gates, T);
-        if (ss.empty()) continue;
-        seg0[li] = (int64_t)segs.size();
-        nseg[li] = (int64_t)ss.size();
-        segs.insert(segs.end(), ss.begin(), ss.end());
-    }
     // upload
     auto al = [](int64_t x) { return (x + 255) & ~(int64_t)255; };
     int64_t b_tg = al((int64_t)tg.size() * (int64_t)sizeof(TileGate));
     int64_t b_m = al((int64_t)mats.size() * (int64_t)sizeof(float4));
     int64_t b_p = al((int64_t)(perms.size() + big_bits.size() + 1) * (int64_t)sizeof(int32_t));
-    int64_t b_s = al((int64_t)(segs.size() + 1) * (int64_t)sizeof(RBSeg));
     int64_t b_tm = al((int64_t)tc_mats.size() * (int64_t)sizeof(double));
     int64_t b_ts = al((int64_t)tc_scale.size() * (int64_t)sizeof(double));
     int64_t b_tc = al(n_var * tc::kPoolBlock * (int64_t)sizeof(uint16_t));   // written on the device
-    const int64_t o_tm = b_tg + b_m + b_p + b_s, o_ts = o_tm + b_tm, o_tc = o_ts + b_ts;
+    const int64_t o_tm = b_tg + b_m + b_p, o_ts = o_tm + b_tm, o_tc = o_ts + b_ts;
     int rc = bs_ensure_plan(s, o_tc + b_tc);
     if (rc) return rc;
     char* host = bs_stage(s, (size_t)o_tc);
@@ -1531,7 +1304,6 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         std::memcpy(host + o_tm, tc_mats.data(), tc_mats.size() * sizeof(double));
         std::memcpy(host + o_ts, tc_scale.data(), tc_scale.size() * sizeof(double));
     }
-    if (!segs.empty()) std::memcpy(host + b_tg + b_m + b_p, segs.data(), segs.size() * sizeof(RBSeg));
     if (!tg.empty()) std::memcpy(host, tg.data(), tg.size() * sizeof(TileGate));
     if (!mats.empty()) std::memcpy(host + b_tg, mats.data(), mats.size() * sizeof(float4));
     if (!perms.empty()) std::memcpy(host + b_tg + b_m, perms.data(), perms.size() * sizeof(int32_t));
@@ -1563,10 +1335,6 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
         attrs((const void*)k_tile_sweep_c64<4>);
         cudaFuncSetAttribute(k_dense_big_c64, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
         cudaFuncSetAttribute(k_dense_big, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-        cudaFuncSetAttribute(k_tile_rb<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-        cudaFuncSetAttribute(k_tile_rb<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-        cudaFuncSetAttribute(k_tile_rb<1>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-        cudaFuncSetAttribute(k_tile_rb<2>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         cudaFuncSetAttribute(k_tile_sweep_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
         cudaFuncSetAttribute(k_tile_sweep_tc, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         attr_set[s->device & 63] = true;
@@ -1588,7 +1356,6 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
     }
     const double esz = c64 ? 8.0 : 16.0;          // bytes per stored amplitude
     const int64_t ntiles = (int64_t)1 << (n_bits - T);
-    const RBSeg* d_seg = (const RBSeg*)(dev + b_tg + b_m + b_p);
     for (size_t li = 0; li < launches.size(); li++) {
         const Launch& ln = launches[li];
         if (ln.big) {
@@ -1647,11 +1414,7 @@ int bs_run_sweeps(bs_sim* s, const std::vector<Sweep>& sweeps) {
                 const size_t sm64 = ((size_t)1 << T) * sizeof(float2) + ((size_t)1 << H) * sizeof(int64_t);
                 if (ln.kmax <= 2) k_tile_sweep_c64<2><<<(unsigned)nb, kThreads, sm64, s->stream>>>((float2*)s->state, d, t0);
                 else k_tile_sweep_c64<4><<<(unsigned)nb, kThreads, sm64, s->stream>>>((float2*)s->state, d, t0);
-            } else if (seg0[li] >= 0 && rb_one)
-                k_tile_rb<1><<<(unsigned)nb, kThreads, smem, s->stream>>>(psi, d, d_seg + seg0[li], (int)nseg[li], t0);
-            else if (seg0[li] >= 0)
-                k_tile_rb<2><<<(unsigned)nb, kThreads, smem, s->stream>>>(psi, d, d_seg + seg0[li], (int)nseg[li], t0);
-            else if (bs_tile_threads(s) == 512) {
+            } else if (bs_tile_threads(s) == 512) {
                 if (ln.kmax <= 2) k_tile_sweep<2, 512><<<(unsigned)nb, 512, smem, s->stream>>>(psi, d, t0);
                 else k_tile_sweep<4, 512><<<(unsigned)nb, 512, smem, s->stream>>>(psi, d, t0);
             } else {

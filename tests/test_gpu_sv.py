@@ -58,8 +58,8 @@ def test_deep_layers(n):
 
 @pytest.mark.parametrize("n", [12, 16, 21])
 def test_one_target_sweeps_with_controls_and_diagonals(n):
-    """Sweeps whose non-diagonal gates are all 1-target (the register-blocked kernel's domain):
-    in-tile and out-of-tile controls, negated controls, monomials and diagonals on far qubits."""
+    """Sweeps whose non-diagonal gates are all 1-target: in-tile and out-of-tile controls, negated
+    controls, monomials and diagonals on far qubits."""
     rng = np.random.default_rng(n + 100)
     ops = []
     for _ in range(80):
